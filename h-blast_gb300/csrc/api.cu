@@ -1,0 +1,873 @@
+// api.cu -- the C ABI (include/hblast_gpu.h): resident database, batches,
+// search launch, ordering and result collection.
+//
+// Replaces H-BLAST's host runtime (h_blast_v1.1/H-BLAST/h_blast.cu): no
+// process-static state, no exit() on error, the database uploaded once and
+// kept resident, every launch on a caller-chosen stream.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../host/batch_builder.h"
+#include "kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CU(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess)                                                    \
+            return fail(HBG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int bits_for(int64_t v) {
+    int b = 0;
+    while (v > 0) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0)
+        n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T));
+}
+
+template <class T>
+void dfree(T *&p) {
+    if (p)
+        cudaFree(p);
+    p = nullptr;
+}
+
+// Device guard: make `dev` current for the scope.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev)
+            cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev)
+            cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+struct hbg_db {
+    int device = 0;
+    int32_t n = 0;
+    int64_t n_res = 0;
+    int64_t letters_len = 0;
+    int32_t max_len = 0;
+    uint8_t *d_letters = nullptr;
+    int64_t *d_off = nullptr;
+    int32_t *d_len = nullptr;
+    int32_t *d_order = nullptr;
+    unsigned long long *d_hist = nullptr;
+    int64_t bytes = 0;
+};
+
+struct hbg_batch {
+    hbg::HostBatch host;
+    int device = -1;
+    HbgGroup *d_groups = nullptr;
+    HbgContext *d_ctx = nullptr;
+    HbgQueryDesc *d_queries = nullptr;
+    uint8_t *d_letters = nullptr;
+    int32_t *d_ctx_of = nullptr;
+    uint32_t *d_cells = nullptr;
+    uint16_t *d_entries = nullptr;
+    uint32_t *d_pv = nullptr;
+    uint16_t *d_qcells = nullptr;
+    int64_t device_bytes = 0;
+};
+
+struct hbg_result {
+    hbg_db *db = nullptr;
+    hbg_batch *batch = nullptr;
+    hbg_gpu_options opt{};
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int64_t cap = 0;
+    int blocks = 0, threads = 256;
+    // device
+    hbg_hsp *d_raw = nullptr, *d_sorted = nullptr;
+    unsigned long long *d_counters = nullptr;  // [0]=hsp count, then per query ext, kept, hits; per group hits
+    unsigned int *d_tile = nullptr;
+    uint32_t *d_gdiag = nullptr;
+    int64_t gdiag_entries = 0;
+    uint64_t *d_keys = nullptr;
+    uint32_t *d_vals = nullptr;
+    uint32_t *d_hist = nullptr;
+    int64_t sort_cap = 0;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // host
+    unsigned long long *h_counters = nullptr;  // pinned
+    size_t n_counters = 0;
+    std::vector<hbg_hsp> hsps;
+    std::vector<hbg_query_stats> stats;
+    std::vector<int64_t> q_first, q_count;
+    int64_t n_hsps = 0;
+    bool launched = false, done = false;
+    float wf_ms = 0.f, ord_ms = 0.f;
+};
+
+namespace {
+
+int upload_batch(hbg_batch *b, int device) {
+    if (b->device == device)
+        return HBG_OK;
+    if (b->device >= 0)
+        return fail(HBG_ERR_STATE, "batch already resident on another device");
+    DeviceScope ds(device);
+    const hbg::HostBatch &h = b->host;
+    CU(dalloc(&b->d_groups, h.groups.size()));
+    CU(dalloc(&b->d_ctx, h.contexts.size()));
+    CU(dalloc(&b->d_queries, h.queries.size()));
+    CU(dalloc(&b->d_letters, h.letters.size() + 64));
+    CU(dalloc(&b->d_ctx_of, h.ctx_of.size() + 16));
+    CU(dalloc(&b->d_cells, h.cells.size()));
+    CU(dalloc(&b->d_entries, h.entries.size() + 8));
+    CU(dalloc(&b->d_pv, h.pv.size()));
+    CU(dalloc(&b->d_qcells, h.query_cells.size()));
+    CU(cudaMemcpy(b->d_groups, h.groups.data(), h.groups.size() * sizeof(HbgGroup), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_ctx, h.contexts.data(), h.contexts.size() * sizeof(HbgContext), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_queries, h.queries.data(), h.queries.size() * sizeof(HbgQueryDesc), cudaMemcpyHostToDevice));
+    CU(cudaMemset(b->d_letters, 0, h.letters.size() + 64));
+    CU(cudaMemcpy(b->d_letters, h.letters.data(), h.letters.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_ctx_of, h.ctx_of.data(), h.ctx_of.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_cells, h.cells.data(), h.cells.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    if (!h.entries.empty())
+        CU(cudaMemcpy(b->d_entries, h.entries.data(), h.entries.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_pv, h.pv.data(), h.pv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_qcells, h.query_cells.data(), h.query_cells.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    b->device_bytes = (int64_t)(h.groups.size() * sizeof(HbgGroup) + h.contexts.size() * sizeof(HbgContext) +
+                                h.queries.size() * sizeof(HbgQueryDesc) + h.letters.size() +
+                                h.ctx_of.size() * 4 + h.cells.size() * 4 + h.entries.size() * 2 +
+                                h.pv.size() * 4 + h.query_cells.size() * 2);
+    b->device = device;
+    return HBG_OK;
+}
+
+void free_result_device(hbg_result *r) {
+    dfree(r->d_raw);
+    dfree(r->d_sorted);
+    dfree(r->d_counters);
+    dfree(r->d_tile);
+    dfree(r->d_gdiag);
+    dfree(r->d_keys);
+    dfree(r->d_vals);
+    dfree(r->d_hist);
+    for (auto &e : r->ev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    if (r->h_counters) {
+        cudaFreeHost(r->h_counters);
+        r->h_counters = nullptr;
+    }
+}
+
+// Allocate (or grow) the result's device buffers for capacity cap.
+int prepare_result(hbg_result *r, int64_t cap) {
+    const hbg::HostBatch &h = r->batch->host;
+    const size_t nq = h.queries.size(), ng = h.groups.size();
+    if (!r->d_counters) {
+        r->n_counters = 1 + 3 * nq + ng;
+        CU(dalloc(&r->d_counters, r->n_counters));
+        CU(cudaMallocHost((void **)&r->h_counters, r->n_counters * sizeof(unsigned long long)));
+        CU(dalloc(&r->d_tile, 1));
+        for (auto &e : r->ev)
+            CU(cudaEventCreate(&e));
+    }
+    if (h.max_diag_len > 0) {
+        const int64_t need = (int64_t)r->blocks * (r->threads / 32) * h.max_diag_len;
+        if (need > r->gdiag_entries) {
+            dfree(r->d_gdiag);
+            CU(dalloc(&r->d_gdiag, (size_t)need));
+            r->gdiag_entries = need;
+        }
+    }
+    if (cap > r->cap) {
+        dfree(r->d_raw);
+        dfree(r->d_sorted);
+        dfree(r->d_keys);
+        dfree(r->d_vals);
+        dfree(r->d_hist);
+        CU(dalloc(&r->d_raw, (size_t)cap));
+        CU(dalloc(&r->d_sorted, (size_t)cap));
+        CU(dalloc(&r->d_keys, (size_t)cap * 2));
+        CU(dalloc(&r->d_vals, (size_t)cap * 2));
+        CU(dalloc(&r->d_hist, (size_t)(256 * hbg::order_max_blocks(cap) + 1)));
+        r->cap = cap;
+    }
+    return HBG_OK;
+}
+
+int launch_search(hbg_result *r) {
+    hbg_db *db = r->db;
+    const hbg::HostBatch &h = r->batch->host;
+    const size_t nq = h.queries.size(), ng = h.groups.size();
+    cudaStream_t st = r->stream;
+    CU(cudaMemsetAsync(r->d_counters, 0, r->n_counters * sizeof(unsigned long long), st));
+    CU(cudaMemsetAsync(r->d_tile, 0, sizeof(unsigned int), st));
+    if (r->d_gdiag)
+        CU(cudaMemsetAsync(r->d_gdiag, 0, (size_t)r->gdiag_entries * sizeof(uint32_t), st));
+
+    hbg::WordFinderArgs a;
+    memset(&a, 0, sizeof(a));
+    a.db = db->d_letters;
+    a.db_off = db->d_off;
+    a.db_len = db->d_len;
+    a.order = db->d_order;
+    a.n_subj = db->n;
+    hbg_batch *b = r->batch;
+    a.groups = b->d_groups;
+    a.n_groups = (int32_t)ng;
+    a.cells = b->d_cells;
+    a.entries = b->d_entries;
+    a.pv = b->d_pv;
+    a.letters = b->d_letters;
+    a.ctx_of = b->d_ctx_of;
+    a.contexts = b->d_ctx;
+    a.queries = b->d_queries;
+    a.window = h.window;
+    a.tile_subjects = 128;
+    a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
+    a.n_tiles = (int64_t)a.tiles_per_group * (int64_t)ng;
+    a.tile_counter = r->d_tile;
+    a.hsps = r->d_raw;
+    a.hsp_count = r->d_counters;
+    a.hsp_cap = r->cap;
+    a.q_extended = r->d_counters + 1;
+    a.q_kept = r->d_counters + 1 + nq;
+    a.g_hits = r->d_counters + 1 + 3 * nq;
+    a.gdiag = r->d_gdiag;
+    a.gdiag_len = h.max_diag_len;
+
+    CU(cudaEventRecord(r->ev[0], st));
+    if (db->n > 0) {
+        CU(hbg::wordfinder_configure());
+        CU(hbg::launch_wordfinder(a, r->blocks, r->threads, st));
+    }
+    CU(cudaEventRecord(r->ev[1], st));
+
+    hbg::OrderArgs o;
+    memset(&o, 0, sizeof(o));
+    o.in = r->d_raw;
+    o.out = r->d_sorted;
+    o.count = r->d_counters;
+    o.cap = r->cap;
+    o.keys[0] = r->d_keys;
+    o.keys[1] = r->d_keys + r->cap;
+    o.vals[0] = r->d_vals;
+    o.vals[1] = r->d_vals + r->cap;
+    o.hist = r->d_hist;
+    o.bits_q = bits_for((int64_t)nq - 1);
+    o.bits_s = bits_for((int64_t)db->n - 1);
+    o.bits_so = bits_for(db->max_len);
+    o.bits_qo = bits_for(h.max_query_len);
+    if (o.bits_q + o.bits_s + o.bits_so + o.bits_qo > 64)
+        return fail(HBG_ERR_TOO_LONG, "ordering key exceeds 64 bits for this database and batch");
+    CU(hbg::launch_order(o, st));
+    CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
+    CU(cudaEventRecord(r->ev[2], st));
+    CU(cudaMemcpyAsync(r->h_counters, r->d_counters, r->n_counters * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, st));
+    r->launched = true;
+    r->done = false;
+    return HBG_OK;
+}
+
+bool valid_opts(const hbg_gpu_options *o) {
+    return o && o->num_threadsx >= 32 && o->num_threadsx <= 256 && (o->num_threadsx % 32) == 0 &&
+           o->num_blocksx >= 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hbg_last_error(void) { return g_err.c_str(); }
+
+int hbg_device_count(int32_t *count) {
+    if (!count)
+        return fail(HBG_ERR_INVALID, "null count");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        *count = 0;
+        return fail(HBG_ERR_NO_DEVICE, cudaGetErrorString(e));
+    }
+    *count = n;
+    return HBG_OK;
+}
+
+int hbg_default_gpu_options(hbg_gpu_options *opt) {
+    if (!opt)
+        return fail(HBG_ERR_INVALID, "null options");
+    opt->use_gpu = 1;
+    opt->num_blocksx = 0;
+    opt->num_threadsx = 256;
+    opt->method = 0;
+    opt->cpu_threads = 1;
+    return HBG_OK;
+}
+
+int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n,
+                const hbg_gpu_options *opt, hbg_db **out) {
+    if (!out || !offsets || n < 0 || (n > 0 && !residues))
+        return fail(HBG_ERR_INVALID, "hbg_db_open: null argument or negative count");
+    *out = nullptr;
+    hbg_gpu_options o;
+    hbg_default_gpu_options(&o);
+    if (opt)
+        o = *opt;
+    if (!o.use_gpu)
+        return fail(HBG_ERR_NO_DEVICE, "use_gpu is 0 and this library has no CPU path");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(HBG_ERR_NO_DEVICE, "no CUDA device");
+    if (o.method < 0 || o.method >= ndev)
+        return fail(HBG_ERR_INVALID, "method selects a device that does not exist");
+    // validate and lay out: one sentinel before every subject and after the last
+    std::vector<int64_t> off(n);
+    std::vector<int32_t> len(n);
+    int64_t pos = 1, total = 0;
+    int32_t max_len = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        int64_t L = offsets[i + 1] - offsets[i];
+        if (L < 0 || L > HBG_MAX_SUBJECT_LEN)
+            return fail(L < 0 ? HBG_ERR_INVALID : HBG_ERR_TOO_LONG,
+                        "subject " + std::to_string(i) + ": bad length");
+        const uint8_t *s = residues + offsets[i];
+        for (int64_t k = 0; k < L; ++k)
+            if (s[k] == 0 || s[k] >= HBG_ALPHABET)
+                return fail(HBG_ERR_INVALID, "subject " + std::to_string(i) +
+                                                 ": letter outside NCBIstdaa 1..27");
+        off[i] = pos;
+        len[i] = (int32_t)L;
+        pos += L + 1;
+        total += L;
+        max_len = std::max<int32_t>(max_len, (int32_t)L);
+    }
+    const int64_t letters_len = pos + 64;
+    std::vector<int32_t> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t x, int32_t y) { return len[x] > len[y]; });
+
+    hbg_db *db = new (std::nothrow) hbg_db;
+    if (!db)
+        return fail(HBG_ERR_NOMEM, "host allocation");
+    db->device = o.method;
+    DeviceScope ds(db->device);
+    auto bail = [&](int code) {
+        dfree(db->d_letters);
+        dfree(db->d_off);
+        dfree(db->d_len);
+        dfree(db->d_order);
+        dfree(db->d_hist);
+        delete db;
+        return code;
+    };
+#define CUB(call)                                                                   \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            return bail(fail(e_ == cudaErrorMemoryAllocation ? HBG_ERR_NOMEM : HBG_ERR_CUDA, \
+                             std::string(#call) + ": " + cudaGetErrorString(e_)));  \
+    } while (0)
+    CUB(dalloc(&db->d_letters, (size_t)letters_len));
+    CUB(dalloc(&db->d_off, (size_t)n));
+    CUB(dalloc(&db->d_len, (size_t)n));
+    CUB(dalloc(&db->d_order, (size_t)n));
+    CUB(dalloc(&db->d_hist, HBG_NUM_CELLS));
+    CUB(cudaMemset(db->d_letters, 0, (size_t)letters_len));
+    // copy subjects with their sentinels through a staging buffer of ~64 MiB
+    {
+        int32_t i = 0;
+        std::vector<uint8_t> stage;
+        while (i < n) {
+            const int64_t start_dev = off[i] - 1;
+            stage.clear();
+            stage.push_back(0);
+            while (i < n && (int64_t)stage.size() < (64 << 20)) {
+                const uint8_t *s = residues + offsets[i];
+                stage.insert(stage.end(), s, s + len[i]);
+                stage.push_back(0);
+                ++i;
+            }
+            CUB(cudaMemcpy(db->d_letters + start_dev, stage.data(), stage.size(), cudaMemcpyHostToDevice));
+        }
+    }
+    if (n > 0) {
+        CUB(cudaMemcpy(db->d_off, off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
+        CUB(cudaMemcpy(db->d_len, len.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        CUB(cudaMemcpy(db->d_order, order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    }
+    CUB(cudaMemset(db->d_hist, 0, sizeof(unsigned long long) * HBG_NUM_CELLS));
+    CUB(hbg::launch_db_histogram(db->d_letters, letters_len, db->d_hist, 0));
+    CUB(cudaDeviceSynchronize());
+#undef CUB
+    db->n = n;
+    db->n_res = total;
+    db->letters_len = letters_len;
+    db->max_len = max_len;
+    db->bytes = letters_len + (int64_t)n * 16 + HBG_NUM_CELLS * 8;
+    *out = db;
+    return HBG_OK;
+}
+
+int hbg_db_close(hbg_db *db) {
+    if (!db)
+        return fail(HBG_ERR_INVALID, "null db");
+    DeviceScope ds(db->device);
+    dfree(db->d_letters);
+    dfree(db->d_off);
+    dfree(db->d_len);
+    dfree(db->d_order);
+    dfree(db->d_hist);
+    delete db;
+    return HBG_OK;
+}
+
+int hbg_db_info(const hbg_db *db, int32_t *n, int64_t *res, int64_t *bytes) {
+    if (!db)
+        return fail(HBG_ERR_INVALID, "null db");
+    if (n)
+        *n = db->n;
+    if (res)
+        *res = db->n_res;
+    if (bytes)
+        *bytes = db->bytes;
+    return HBG_OK;
+}
+
+static int finish_batch(std::vector<hbg::QueryIn> &qs, const hbg_word_params *params,
+                        int32_t max_group_len, hbg_batch **out) {
+    hbg_batch *b = new (std::nothrow) hbg_batch;
+    if (!b)
+        return fail(HBG_ERR_NOMEM, "host allocation");
+    std::string err = hbg::build_batch(qs, params->threshold, params->window, max_group_len, &b->host);
+    if (!err.empty()) {
+        delete b;
+        return fail(err.find("length") != std::string::npos ? HBG_ERR_TOO_LONG : HBG_ERR_INVALID, err);
+    }
+    *out = b;
+    return HBG_OK;
+}
+
+int hbg_batch_create(const hbg_query *queries, int32_t n_queries, const hbg_word_params *params,
+                     int32_t max_group_len, hbg_batch **out) {
+    if (!out || !params || !queries || n_queries <= 0)
+        return fail(HBG_ERR_INVALID, "hbg_batch_create: null argument or empty batch");
+    *out = nullptr;
+    std::vector<hbg::QueryIn> qs(n_queries);
+    for (int32_t k = 0; k < n_queries; ++k) {
+        const hbg_query &q = queries[k];
+        if (!q.sequence || q.num_contexts <= 0 || !q.context_offset || !q.context_length ||
+            !q.x_dropoff || !q.cutoff_score)
+            return fail(HBG_ERR_INVALID, "query " + std::to_string(k) + ": null field");
+        qs[k].seq = q.sequence;
+        qs[k].len = q.length;
+        qs[k].ctx_off.assign(q.context_offset, q.context_offset + q.num_contexts);
+        qs[k].ctx_len.assign(q.context_length, q.context_length + q.num_contexts);
+        qs[k].xdrop.assign(q.x_dropoff, q.x_dropoff + q.num_contexts);
+        qs[k].cutoff.assign(q.cutoff_score, q.cutoff_score + q.num_contexts);
+    }
+    return finish_batch(qs, params, max_group_len, out);
+}
+
+int hbg_batch_create_blastx(const uint8_t *const *nt, const int32_t *nt_len, int32_t n_queries,
+                            const int32_t *x_dropoff, const int32_t *cutoff,
+                            const hbg_word_params *params, int32_t max_group_len, hbg_batch **out) {
+    if (!out || !params || !nt || !nt_len || !x_dropoff || !cutoff || n_queries <= 0)
+        return fail(HBG_ERR_INVALID, "hbg_batch_create_blastx: null argument or empty batch");
+    *out = nullptr;
+    std::vector<std::vector<uint8_t>> prot(n_queries);
+    std::vector<hbg::QueryIn> qs(n_queries);
+    for (int32_t k = 0; k < n_queries; ++k) {
+        if (!nt[k] || nt_len[k] < 3)
+            return fail(HBG_ERR_INVALID, "query " + std::to_string(k) + ": need >= 3 nucleotides");
+        if ((int64_t)nt_len[k] * 2 + 6 > HBG_MAX_QUERY_LEN)
+            return fail(HBG_ERR_TOO_LONG, "query " + std::to_string(k) + ": too long");
+        prot[k] = hbg::translate_six_frames(nt[k], nt_len[k], &qs[k].ctx_off, &qs[k].ctx_len);
+        qs[k].seq = prot[k].data();
+        qs[k].len = qs[k].ctx_off[5] + qs[k].ctx_len[5];
+        qs[k].xdrop.assign(x_dropoff + 6 * k, x_dropoff + 6 * k + 6);
+        qs[k].cutoff.assign(cutoff + 6 * k, cutoff + 6 * k + 6);
+        // translated letters may include the sentinel-free stop '*' (25): allowed
+    }
+    return finish_batch(qs, params, max_group_len, out);
+}
+
+int hbg_batch_create_from_smallbone(const hbg_query *query, const hbg_word_params *params,
+                                    const void *backbone, int32_t backbone_size,
+                                    const uint16_t *overflow, int64_t overflow_size,
+                                    hbg_batch **out) {
+    if (!out || !params || !query || !backbone || backbone_size <= 0 ||
+        backbone_size > HBG_NUM_CELLS || overflow_size < 0 || (overflow_size > 0 && !overflow))
+        return fail(HBG_ERR_INVALID, "hbg_batch_create_from_smallbone: bad argument");
+    int rc = hbg_batch_create(query, 1, params, 1, out);
+    if (rc != HBG_OK)
+        return rc;
+    hbg::HostBatch &h = (*out)->host;
+    // NCBI AaLookupSmallboneCell: Int4 num_used; union { Uint2 entries[3]; Int4 cursor; }
+    struct Cell {
+        int32_t num_used;
+        union {
+            uint16_t entries[3];
+            int32_t cursor;
+        } payload;
+    };
+    const Cell *cells = (const Cell *)backbone;
+    std::vector<uint32_t> cs(HBG_CELL_STRIDE, 0);
+    std::vector<uint16_t> ents;
+    std::vector<uint32_t> pv(HBG_PV_WORDS, 0);
+    std::vector<uint16_t> qc(HBG_NUM_CELLS, 0);
+    const int32_t qlen = query->length;
+    for (int32_t w = 0; w < HBG_NUM_CELLS; ++w) {
+        cs[w] = (uint32_t)ents.size();
+        if (w >= backbone_size)
+            continue;
+        const Cell &c = cells[w];
+        if (c.num_used < 0)
+            goto bad;
+        if (c.num_used == 0)
+            continue;
+        {
+            std::vector<uint16_t> v;
+            if (c.num_used <= 3) {
+                v.assign(c.payload.entries, c.payload.entries + c.num_used);
+            } else {
+                if (c.payload.cursor < 0 || (int64_t)c.payload.cursor + c.num_used > overflow_size)
+                    goto bad;
+                v.assign(overflow + c.payload.cursor, overflow + c.payload.cursor + c.num_used);
+            }
+            std::sort(v.begin(), v.end());
+            for (uint16_t x : v)
+                if ((int32_t)x + HBG_WORD_SIZE > qlen)
+                    goto bad;
+            ents.insert(ents.end(), v.begin(), v.end());
+            pv[w >> 5] |= 1u << (w & 31);
+            qc[w] = (uint16_t)c.num_used;
+        }
+    }
+    cs[HBG_NUM_CELLS] = (uint32_t)ents.size();
+    h.cells = cs;
+    h.entries = ents;
+    h.pv = pv;
+    h.query_cells = qc;
+    h.groups[0].entry_base = 0;
+    return HBG_OK;
+bad:
+    hbg_batch_destroy(*out);
+    *out = nullptr;
+    return fail(HBG_ERR_INVALID, "smallbone table: bad cell");
+}
+
+int hbg_batch_lookup_table(const hbg_batch *b, int32_t g, uint32_t *cells, uint16_t *entries,
+                           int64_t entries_cap, int64_t *n_entries, int32_t *first_query,
+                           int32_t *n_queries, int32_t *query_start) {
+    if (!b || !n_entries || g < 0 || g >= (int32_t)b->host.groups.size())
+        return fail(HBG_ERR_INVALID, "hbg_batch_lookup_table: bad argument");
+    const hbg::HostBatch &h = b->host;
+    const HbgGroup &G = h.groups[g];
+    const uint32_t *cs = h.cells.data() + (size_t)g * HBG_CELL_STRIDE;
+    const int64_t n = cs[HBG_NUM_CELLS];
+    *n_entries = n;
+    if (first_query)
+        *first_query = G.first_query;
+    if (n_queries)
+        *n_queries = G.n_queries;
+    if (query_start)
+        for (int32_t k = 0; k < G.n_queries; ++k)
+            query_start[k] = h.queries[G.first_query + k].start;
+    if (cells)
+        memcpy(cells, cs, sizeof(uint32_t) * HBG_CELL_STRIDE);
+    if (entries) {
+        if (entries_cap < n)
+            return fail(HBG_ERR_CAPACITY, "entries buffer too small");
+        if (n)
+            memcpy(entries, h.entries.data() + G.entry_base, sizeof(uint16_t) * (size_t)n);
+    }
+    return HBG_OK;
+}
+
+int hbg_batch_destroy(hbg_batch *b) {
+    if (!b)
+        return fail(HBG_ERR_INVALID, "null batch");
+    if (b->device >= 0) {
+        DeviceScope ds(b->device);
+        dfree(b->d_groups);
+        dfree(b->d_ctx);
+        dfree(b->d_queries);
+        dfree(b->d_letters);
+        dfree(b->d_ctx_of);
+        dfree(b->d_cells);
+        dfree(b->d_entries);
+        dfree(b->d_pv);
+        dfree(b->d_qcells);
+    }
+    delete b;
+    return HBG_OK;
+}
+
+int hbg_batch_info(const hbg_batch *b, int32_t *nq, int32_t *ng, int64_t *qlen, int64_t *entries) {
+    if (!b)
+        return fail(HBG_ERR_INVALID, "null batch");
+    if (nq)
+        *nq = (int32_t)b->host.queries.size();
+    if (ng)
+        *ng = (int32_t)b->host.groups.size();
+    if (qlen) {
+        int64_t t = 0;
+        for (auto &q : b->host.queries)
+            t += q.len;
+        *qlen = t;
+    }
+    if (entries)
+        *entries = (int64_t)b->host.entries.size();
+    return HBG_OK;
+}
+
+int hbg_mem_required(const hbg_db *db, const hbg_batch *b, int64_t cap, int64_t *bytes) {
+    if (!db || !b || !bytes || cap < 0)
+        return fail(HBG_ERR_INVALID, "hbg_mem_required: bad argument");
+    if (cap == 0)
+        cap = std::max<int64_t>(1 << 20, (int64_t)db->n * 20);
+    const hbg::HostBatch &h = b->host;
+    int64_t batch_bytes = (int64_t)(h.letters.size() + h.ctx_of.size() * 4 + h.cells.size() * 4 +
+                                    h.entries.size() * 2 + h.pv.size() * 4 + h.query_cells.size() * 2);
+    int64_t per_hsp = 2 * (int64_t)sizeof(hbg_hsp) + 2 * 8 + 2 * 4;
+    int64_t gdiag = 0;
+    if (h.max_diag_len > 0) {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
+        gdiag = (int64_t)sms * 8 * 8 * h.max_diag_len * 4;
+    }
+    *bytes = batch_bytes + cap * per_hsp + gdiag + 1024 * 1024;
+    return HBG_OK;
+}
+
+int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t cap,
+               void *stream, hbg_result **out) {
+    if (!db || !batch || !out || cap < 0)
+        return fail(HBG_ERR_INVALID, "hbg_search: null argument");
+    hbg_gpu_options o;
+    hbg_default_gpu_options(&o);
+    if (opt)
+        o = *opt;
+    if (!o.use_gpu)
+        return fail(HBG_ERR_NO_DEVICE, "use_gpu is 0 and this library has no CPU path");
+    if (!valid_opts(&o))
+        return fail(HBG_ERR_INVALID, "num_threadsx must be a multiple of 32 in 32..256");
+    DeviceScope ds(db->device);
+    int rc = upload_batch(batch, db->device);
+    if (rc != HBG_OK)
+        return rc;
+    hbg_result *r = *out;
+    if (r && (r->db != db || r->batch != batch)) {
+        return fail(HBG_ERR_STATE, "a reused result must belong to the same database and batch");
+    }
+    if (!r) {
+        r = new (std::nothrow) hbg_result;
+        if (!r)
+            return fail(HBG_ERR_NOMEM, "host allocation");
+        r->db = db;
+        r->batch = batch;
+        r->device = db->device;
+    }
+    r->opt = o;
+    r->stream = (cudaStream_t)stream;
+    r->threads = o.num_threadsx;
+    if (o.num_blocksx > 0) {
+        r->blocks = o.num_blocksx;
+    } else {
+        int sms = 1, per = 1;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
+        if (hbg::wordfinder_configure() != cudaSuccess) {
+            if (!*out)
+                delete r;
+            return fail(HBG_ERR_CUDA, "cannot configure the word-finder kernel (wrong GPU?)");
+        }
+        if (hbg::wordfinder_occupancy(r->threads, &per) != cudaSuccess || per < 1)
+            per = 1;
+        r->blocks = sms * per;
+    }
+    if (cap == 0)
+        cap = std::max<int64_t>(1 << 20, (int64_t)db->n * 20);
+    rc = prepare_result(r, std::max<int64_t>(cap, r->cap));
+    if (rc == HBG_OK)
+        rc = launch_search(r);
+    if (rc != HBG_OK) {
+        if (!*out) {
+            free_result_device(r);
+            delete r;
+        }
+        return rc;
+    }
+    *out = r;
+    return HBG_OK;
+}
+
+int hbg_result_wait(hbg_result *r) {
+    if (!r || !r->launched)
+        return fail(HBG_ERR_STATE, "no search launched on this result");
+    if (r->done)
+        return HBG_OK;
+    DeviceScope ds(r->device);
+    CU(cudaStreamSynchronize(r->stream));
+    unsigned long long n = r->h_counters[0];
+    if ((int64_t)n > r->cap) {
+        // the HSP buffer was too small: relaunch once with the exact size
+        int rc = prepare_result(r, (int64_t)n);
+        if (rc != HBG_OK)
+            return rc;
+        rc = launch_search(r);
+        if (rc != HBG_OK)
+            return rc;
+        CU(cudaStreamSynchronize(r->stream));
+        n = r->h_counters[0];
+        if ((int64_t)n > r->cap)
+            return fail(HBG_ERR_STATE, "HSP count changed between identical launches");
+    }
+    r->n_hsps = (int64_t)n;
+    CU(cudaEventElapsedTime(&r->wf_ms, r->ev[0], r->ev[1]));
+    CU(cudaEventElapsedTime(&r->ord_ms, r->ev[1], r->ev[2]));
+    r->hsps.resize((size_t)n);
+    if (n)
+        CU(cudaMemcpy(r->hsps.data(), r->d_sorted, (size_t)n * sizeof(hbg_hsp), cudaMemcpyDeviceToHost));
+    const size_t nq = r->batch->host.queries.size();
+    r->stats.assign(nq, hbg_query_stats{0, 0, 0, 0});
+    r->q_first.assign(nq, 0);
+    r->q_count.assign(nq, 0);
+    for (size_t q = 0; q < nq; ++q) {
+        r->stats[q].init_extends = (int64_t)r->h_counters[1 + q];
+        r->stats[q].good_init_extends = (int64_t)r->h_counters[1 + nq + q];
+        r->stats[q].lookup_hits = (int64_t)r->h_counters[1 + 2 * nq + q];
+    }
+    // per-query ranges and subjects with HSPs (the list is ordered by query, subject)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const hbg_hsp &h = r->hsps[(size_t)i];
+        if (r->q_count[h.query] == 0)
+            r->q_first[h.query] = i;
+        r->q_count[h.query]++;
+        if (i == 0 || r->hsps[(size_t)i - 1].query != h.query || r->hsps[(size_t)i - 1].subject != h.subject)
+            r->stats[h.query].subjects_passed++;
+    }
+    r->done = true;
+    return HBG_OK;
+}
+
+int hbg_result_timing(const hbg_result *r, float *wf, float *ord) {
+    if (!r || !r->done)
+        return fail(HBG_ERR_STATE, "result not collected");
+    if (wf)
+        *wf = r->wf_ms;
+    if (ord)
+        *ord = r->ord_ms;
+    return HBG_OK;
+}
+
+int hbg_result_counts(const hbg_result *r, int64_t *n_hsps, int32_t *n_queries) {
+    if (!r || !r->done)
+        return fail(HBG_ERR_STATE, "result not collected");
+    if (n_hsps)
+        *n_hsps = r->n_hsps;
+    if (n_queries)
+        *n_queries = (int32_t)r->batch->host.queries.size();
+    return HBG_OK;
+}
+
+int hbg_result_hsps(const hbg_result *r, int64_t first, int64_t count, hbg_hsp *out) {
+    if (!r || !r->done)
+        return fail(HBG_ERR_STATE, "result not collected");
+    if (first < 0 || count < 0 || first + count > r->n_hsps || (count > 0 && !out))
+        return fail(HBG_ERR_INVALID, "range outside the result");
+    if (count)
+        memcpy(out, r->hsps.data() + first, (size_t)count * sizeof(hbg_hsp));
+    return HBG_OK;
+}
+
+int hbg_result_query_range(const hbg_result *r, int32_t q, int64_t *first, int64_t *count) {
+    if (!r || !r->done)
+        return fail(HBG_ERR_STATE, "result not collected");
+    if (q < 0 || q >= (int32_t)r->q_first.size() || !first || !count)
+        return fail(HBG_ERR_INVALID, "query index outside the batch");
+    *first = r->q_first[q];
+    *count = r->q_count[q];
+    return HBG_OK;
+}
+
+int hbg_result_stats(const hbg_result *r, int32_t q, hbg_query_stats *out) {
+    if (!r || !r->done)
+        return fail(HBG_ERR_STATE, "result not collected");
+    if (q < 0 || q >= (int32_t)r->stats.size() || !out)
+        return fail(HBG_ERR_INVALID, "query index outside the batch");
+    *out = r->stats[q];
+    return HBG_OK;
+}
+
+int hbg_result_free(hbg_result *r) {
+    if (!r)
+        return fail(HBG_ERR_INVALID, "null result");
+    DeviceScope ds(r->device);
+    if (r->launched && !r->done)
+        cudaStreamSynchronize(r->stream);
+    free_result_device(r);
+    delete r;
+    return HBG_OK;
+}
+
+int hbg_search_sync(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, hbg_hsp *out,
+                    int64_t out_cap, int64_t *n_hsps, hbg_query_stats *stats, void *stream) {
+    if (!n_hsps || out_cap < 0)
+        return fail(HBG_ERR_INVALID, "hbg_search_sync: bad argument");
+    hbg_result *r = nullptr;
+    int rc = hbg_search(db, batch, opt, 0, stream, &r);
+    if (rc != HBG_OK)
+        return rc;
+    rc = hbg_result_wait(r);
+    if (rc == HBG_OK) {
+        *n_hsps = r->n_hsps;
+        if (stats)
+            for (size_t q = 0; q < r->stats.size(); ++q)
+                stats[q] = r->stats[q];
+        if (out) {
+            if (r->n_hsps > out_cap)
+                rc = fail(HBG_ERR_CAPACITY, "output buffer too small");
+            else if (r->n_hsps)
+                memcpy(out, r->hsps.data(), (size_t)r->n_hsps * sizeof(hbg_hsp));
+        }
+    }
+    hbg_result_free(r);
+    return rc;
+}
+
+}  // extern "C"

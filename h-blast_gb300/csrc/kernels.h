@@ -1,0 +1,82 @@
+// kernels.h -- launch wrappers of the device code (host-callable).
+#ifndef HBG_KERNELS_H
+#define HBG_KERNELS_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hbg_internal.h"
+
+namespace hbg {
+
+struct WordFinderArgs {
+    // resident database
+    const uint8_t *db;            // letters, one sentinel between subjects
+    const int64_t *db_off;        // start of subject i
+    const int32_t *db_len;        // length of subject i
+    const int32_t *order;         // scheduling order of subjects (longest first)
+    int32_t n_subj;
+    // batch
+    const HbgGroup *groups;
+    int32_t n_groups;
+    const uint32_t *cells;        // n_groups x HBG_CELL_STRIDE
+    const uint16_t *entries;
+    const uint32_t *pv;           // n_groups x HBG_PV_WORDS
+    const uint8_t *letters;
+    const int32_t *ctx_of;
+    const HbgContext *contexts;
+    const HbgQueryDesc *queries;
+    int32_t window;
+    // scheduling: tile t covers group t / tiles_per_group and scheduled
+    // subjects [(t % tiles_per_group) * tile_subjects, ... + tile_subjects)
+    int32_t tile_subjects;
+    int32_t tiles_per_group;
+    int64_t n_tiles;
+    unsigned int *tile_counter;   // zeroed before launch
+    // outputs
+    hbg_hsp *hsps;
+    unsigned long long *hsp_count;  // zeroed before launch
+    int64_t hsp_cap;
+    unsigned long long *q_extended; // per batch query, zeroed
+    unsigned long long *q_kept;     // per batch query, zeroed
+    unsigned long long *g_hits;     // per group lookup hits, zeroed
+    // global-memory diagonal tables (groups with placement 1): one slice of
+    // gdiag_len entries per (block, warp), zeroed before launch
+    uint32_t *gdiag;
+    int32_t gdiag_len;
+};
+
+// Shared memory the word-finder kernel needs for a CTA of `threads` threads.
+size_t wordfinder_smem_bytes(int threads);
+cudaError_t wordfinder_configure();
+cudaError_t wordfinder_occupancy(int threads, int *blocks_per_sm);
+cudaError_t launch_wordfinder(const WordFinderArgs &a, int blocks, int threads,
+                              cudaStream_t stream);
+
+// Ordering pass: sort HSPs by (query, subject, s_off, q_off).
+struct OrderArgs {
+    const hbg_hsp *in;
+    hbg_hsp *out;
+    const unsigned long long *count;  // device count of HSPs (clamped to cap)
+    int64_t cap;
+    uint64_t *keys[2];
+    uint32_t *vals[2];
+    uint32_t *hist;                   // 256 x max_blocks
+    int bits_q, bits_s, bits_so, bits_qo;
+};
+int64_t order_max_blocks(int64_t cap);
+cudaError_t launch_order(const OrderArgs &a, cudaStream_t stream);
+
+// Database word histogram: hist[w] += positions whose three letters are
+// non-sentinel and form word w.
+cudaError_t launch_db_histogram(const uint8_t *db, int64_t n, unsigned long long *hist,
+                                cudaStream_t stream);
+
+// lookup_hits[q] = sum_w hist[w] * query_cells[q][w]
+cudaError_t launch_query_hits(const unsigned long long *hist, const uint16_t *query_cells,
+                              int32_t n_queries, unsigned long long *out,
+                              cudaStream_t stream);
+
+}  // namespace hbg
+
+#endif

@@ -1,0 +1,61 @@
+// batch_builder.h -- host-side construction of a query batch: query packing
+// into groups, six-frame translation for BLASTX, and the neighbourhood-word
+// lookup tables.  Pure C++ (no CUDA); the runtime uploads the result.
+#ifndef HBG_BATCH_BUILDER_H
+#define HBG_BATCH_BUILDER_H
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../csrc/hbg_internal.h"
+
+namespace hbg {
+
+// Shared-memory diagonal tables hold at most this many entries per warp;
+// groups whose table is longer use the global-memory scratch.
+constexpr int32_t kSmemDiagLen = 2048;
+// Queries per group are bounded so per-query counters fit in shared memory.
+constexpr int32_t kMaxQueriesPerGroup = 64;
+
+struct HostBatch {
+    int32_t threshold = 11;
+    int32_t window = 40;
+    std::vector<HbgGroup> groups;
+    std::vector<HbgContext> contexts;
+    std::vector<HbgQueryDesc> queries;
+    std::vector<uint8_t> letters;        // all groups, gaps included
+    std::vector<int32_t> ctx_of;         // per letter, -1 outside contexts
+    std::vector<uint32_t> cells;         // groups x HBG_CELL_STRIDE
+    std::vector<uint16_t> entries;       // group-local query offsets
+    std::vector<uint32_t> pv;            // groups x HBG_PV_WORDS
+    std::vector<uint16_t> query_cells;   // queries x HBG_NUM_CELLS cell sizes
+    int32_t max_query_len = 0;
+    int32_t max_diag_len = 0;            // over groups with global placement
+};
+
+// One query already in NCBI concatenated form.
+struct QueryIn {
+    const uint8_t *seq;
+    int32_t len;
+    std::vector<int32_t> ctx_off, ctx_len, xdrop, cutoff;
+};
+
+// Returns an empty string on success, else the reason.
+std::string build_batch(const std::vector<QueryIn> &queries, int32_t threshold,
+                        int32_t window, int32_t max_group_len, HostBatch *out);
+
+// Standard-code six-frame translation (frames +1,+2,+3,-1,-2,-3, one sentinel
+// between frames).  Returns the concatenated letters; fills offsets/lengths.
+std::vector<uint8_t> translate_six_frames(const uint8_t *nt, int32_t nt_len,
+                                          std::vector<int32_t> *ctx_off,
+                                          std::vector<int32_t> *ctx_len);
+
+// Substitution score of NCBIstdaa letters (BLOSUM62).
+int32_t blosum62(int32_t a, int32_t b);
+const int8_t *blosum62_table();   // 28 rows x 32 columns, row = query letter
+
+}  // namespace hbg
+
+#endif

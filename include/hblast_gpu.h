@@ -1,0 +1,263 @@
+/*
+ * hblast_gpu.h -- C ABI of the GB300 word-hit stage (BLASTP/BLASTX lookup,
+ * two-hit diagonal detection, ungapped X-drop extension).
+ *
+ * Plain C types only: pointers, sizes, int32/int64.  Every call returns an
+ * int status (HBG_OK or a negative HBG_ERR_* code); nothing here exits the
+ * process or resets a device.  Handles are independent: a process may hold
+ * several databases and batches, and calls on different handles may run from
+ * different host threads.
+ *
+ * Each entry point names the H-BLAST interface it replaces.  H-BLAST paths are
+ * inside h_blast_v1.1/H-BLAST/ (NF = ncbi_blast_files/).
+ */
+#ifndef HBLAST_GPU_H
+#define HBLAST_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define HBG_OK 0
+#define HBG_ERR_INVALID -1      /* bad argument (null pointer, bad size, bad residue) */
+#define HBG_ERR_CUDA -2         /* a CUDA runtime call failed; see hbg_last_error() */
+#define HBG_ERR_NOMEM -3        /* host or device allocation failed */
+#define HBG_ERR_TOO_LONG -4     /* a query or subject exceeds a documented limit */
+#define HBG_ERR_NO_DEVICE -5    /* no CUDA device, or the library was built for another GPU */
+#define HBG_ERR_STATE -6        /* call out of order (e.g. collect before search) */
+#define HBG_ERR_CAPACITY -7     /* a caller-sized buffer is too small; the needed size is reported */
+
+/* ---- limits ------------------------------------------------------------- */
+#define HBG_WORD_SIZE 3
+#define HBG_NUM_CELLS 32768            /* 1 << (5 bits x 3 letters) */
+#define HBG_ALPHABET 28                /* NCBIstdaa letters 0..27 */
+#define HBG_MAX_QUERY_LEN 65000        /* concatenated contexts of one query */
+#define HBG_MAX_SUBJECT_LEN 1000000000 /* subjects are int32-indexed */
+
+/* ---- records ------------------------------------------------------------ */
+
+/* One ungapped HSP.  Offsets are local to the query (its contexts
+ * concatenated NCBI-style, one sentinel between contexts) and to the subject.
+ * Replaces GPUBlastInitHitList (NF/gpu_cpu_common.h:31-40): int32 fields
+ * instead of uint16, the hit offset stored directly instead of
+ * offset_from_first_position, and the query/subject/context written out.
+ * BlastSaveInitHsp(list, q_start, s_start, q_off, s_off, len, score) takes
+ * these fields as they are (NF/blast_engine.c:567-576). */
+typedef struct hbg_hsp {
+    int32_t query;     /* index of the query in its batch */
+    int32_t subject;   /* ordinal id of the subject in the database */
+    int32_t q_start;   /* first query residue of the HSP */
+    int32_t s_start;   /* first subject residue of the HSP */
+    int32_t q_off;     /* query offset of the word hit that triggered it */
+    int32_t s_off;     /* subject offset of that word hit */
+    int32_t len;       /* HSP length */
+    int32_t score;     /* raw ungapped score */
+    int32_t context;   /* context of the query (0 for blastp, frame 0..5 for blastx) */
+} hbg_hsp;
+
+/* Per-query diagnostics, the numbers NCBI feeds to Blast_UngappedStatsUpdate
+ * (NF/blast_engine.c:579-582) summed over the database. */
+typedef struct hbg_query_stats {
+    int64_t lookup_hits;       /* word hits found by the scan */
+    int64_t init_extends;      /* ungapped extensions tried */
+    int64_t good_init_extends; /* extensions that reached the cutoff */
+    int64_t subjects_passed;   /* subjects with at least one HSP */
+} hbg_query_stats;
+
+/* One query as NCBI concatenates it (BLAST_SequenceBlk + BlastQueryInfo,
+ * read by H-BLAST at h_blast.cu:968-983): residues in NCBIstdaa, contexts in
+ * order, one sentinel (0) between consecutive contexts; length =
+ * context_offset[last] + context_length[last].  x_dropoff and cutoff_score
+ * are per context in raw score units (word_params->cutoffs[ctx], read at
+ * h_blast.cu:977-983). */
+typedef struct hbg_query {
+    const uint8_t *sequence;
+    int32_t length;
+    int32_t num_contexts;
+    const int32_t *context_offset;
+    const int32_t *context_length;
+    const int32_t *x_dropoff;
+    const int32_t *cutoff_score;
+} hbg_query;
+
+/* Word-finder parameters (LookupTableOptions + the diagonal window). */
+typedef struct hbg_word_params {
+    int32_t threshold;   /* neighbourhood threshold T (11 for blastp/blastx) */
+    int32_t window;      /* two-hit window A (40) */
+} hbg_word_params;
+
+/* Mirror of BlastGPUOptions (NF/blast_options.h:503-514), the values of the
+ * -gpu, -gpu_threads, -gpu_blocks, -method and -num_threads flags
+ * (NF/blast_args.cpp:2705-2778).  num_threadsx is the CTA size (a multiple
+ * of 32, 32..1024); num_blocksx 0 means one persistent wave sized from the
+ * SM count; method selects the device among the visible ones (0 = first);
+ * use_gpu 0 makes hbg_search return HBG_ERR_NO_DEVICE (this library has no
+ * CPU path). */
+typedef struct hbg_gpu_options {
+    int32_t use_gpu;
+    int32_t num_blocksx;
+    int32_t num_threadsx;
+    int32_t method;
+    int32_t cpu_threads;
+} hbg_gpu_options;
+
+/* Values of the H-BLAST_runtime_options text file
+ * (runtime_setting_files/H-BLAST_runtime_options:1-18, parsed by
+ * NF/functions.cpp:142-202).  avg_hsps_per_sequence sizes the HSP buffer;
+ * the other values drive H-BLAST's CPU/GPU balancer and are kept readable
+ * for compatibility. */
+typedef struct hbg_runtime_options {
+    double gpu_db_used_ratio;
+    int32_t fixed_ratio;
+    double ccr;
+    int32_t avg_hsps_per_sequence;
+    int32_t mem_ecc;
+    int32_t balancer_method;
+    int32_t load_factor;
+    int32_t chunk_size;
+    int32_t base_value;
+} hbg_runtime_options;
+
+typedef struct hbg_db hbg_db;         /* device-resident subject database */
+typedef struct hbg_batch hbg_batch;   /* packed queries + lookup tables */
+typedef struct hbg_result hbg_result; /* one search: device buffers + host copy */
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Text of the last error on the calling thread ("" if none). */
+const char *hbg_last_error(void);
+
+/* Number of usable devices (replaces GPU_BLAST_check_availability,
+ * NF/gpu_cpu_common.h:103, and gpu_get_device_count). */
+int hbg_device_count(int32_t *count);
+
+/* Defaults: use_gpu 1, num_blocksx 0, num_threadsx 256, method 0,
+ * cpu_threads 1 (cf. NF/cmdline_flags.cpp:215-228). */
+int hbg_default_gpu_options(hbg_gpu_options *opt);
+
+/* Parse an H-BLAST_runtime_options file: comment/value line pairs in the
+ * order of runtime_setting_files/H-BLAST_runtime_options, with the same
+ * range fix-ups as Read_H_BLAST_runtime_options (NF/functions.cpp:142-202).
+ * A missing file gives the defaults and HBG_OK (the reference prints a
+ * warning and keeps its defaults). */
+int hbg_read_runtime_options(const char *path, hbg_runtime_options *out);
+
+/* ---- database ----------------------------------------------------------- */
+
+/* Copy n_subjects protein sequences to device memory and keep them resident.
+ * Subject i is residues[offsets[i] .. offsets[i+1]) (offsets has n_subjects+1
+ * entries), NCBIstdaa letters 1..27.  Replaces the per-volume .hDb staging
+ * of Read_H_BLAST_GPU_DB + H_BLAST's database copy (h_blast.cu:587-653,
+ * 993, 1094-1096): the database is packed uint8 with one sentinel between
+ * subjects plus an int64 offset array, uploaded once. */
+int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n_subjects,
+                const hbg_gpu_options *opt, hbg_db **out);
+int hbg_db_close(hbg_db *db);
+int hbg_db_info(const hbg_db *db, int32_t *n_subjects, int64_t *n_residues,
+                int64_t *device_bytes);
+
+/* ---- query batches -------------------------------------------------------- */
+
+/* Build the neighbourhood lookup tables of a batch of protein queries on the
+ * host (the work NCBI's BlastAaLookupTableNew/BlastAaLookupIndexQuery do
+ * before H-BLAST reads the table at h_blast.cu:940-958, with cells sorted as
+ * lut_sorting does at h_blast.cu:165-194).  Queries are packed into groups
+ * that share one scan of the database; results are identical to searching
+ * each query alone.  max_group_len 0 = library default; 1 packs one query
+ * per group (the plain one-query-per-launch form). */
+int hbg_batch_create(const hbg_query *queries, int32_t n_queries,
+                     const hbg_word_params *params, int32_t max_group_len,
+                     hbg_batch **out);
+
+/* BLASTX batch: nucleotide queries (A=0 C=1 G=2 T=3, other = N) are
+ * translated in six frames with the standard genetic code while the lookup
+ * tables are built; contexts are frames +1,+2,+3,-1,-2,-3.  x_dropoff and
+ * cutoff_score hold 6 values per query. */
+int hbg_batch_create_blastx(const uint8_t *const *nt_sequences, const int32_t *nt_lengths,
+                            int32_t n_queries, const int32_t *x_dropoff,
+                            const int32_t *cutoff_score, const hbg_word_params *params,
+                            int32_t max_group_len, hbg_batch **out);
+
+/* Use a lookup table the caller already has in NCBI's small-backbone layout
+ * for one query (the table H_BLAST copies at h_blast.cu:953-958):
+ * backbone[i] = {num_used, payload} cells of 8 bytes (payload = 3 uint16
+ * offsets when num_used <= 3, else an int32 cursor into overflow),
+ * backbone_size cells.  Cells are used in ascending order of offset, the order
+ * lut_sorting produces. */
+int hbg_batch_create_from_smallbone(const hbg_query *query, const hbg_word_params *params,
+                                    const void *backbone, int32_t backbone_size,
+                                    const uint16_t *overflow, int64_t overflow_size,
+                                    hbg_batch **out);
+
+/* Export group g's lookup table in CSR form: cells[w] .. cells[w+1] index
+ * entries (group-local query offsets, ascending).  cells holds
+ * HBG_NUM_CELLS + 1 values; *n_entries receives the entry count, and
+ * HBG_ERR_CAPACITY is returned when entries_cap is smaller.  Also reports the
+ * group's first query and each of its queries' start inside the group via
+ * query_start (n_queries values, may be NULL).  The NCBI table H-BLAST reads
+ * (h_blast.cu:940-958) carries the same cells. */
+int hbg_batch_lookup_table(const hbg_batch *batch, int32_t g, uint32_t *cells,
+                           uint16_t *entries, int64_t entries_cap, int64_t *n_entries,
+                           int32_t *first_query, int32_t *n_queries, int32_t *query_start);
+
+int hbg_batch_destroy(hbg_batch *batch);
+int hbg_batch_info(const hbg_batch *batch, int32_t *n_queries, int32_t *n_groups,
+                   int64_t *total_query_len, int64_t *lookup_entries);
+
+/* Estimate of the device bytes one search of batch against db needs beyond
+ * the resident database (replaces H_BLAST_check_memory, h_blast.cu:1280-1349).
+ * hsp_capacity 0 = default sizing. */
+int hbg_mem_required(const hbg_db *db, const hbg_batch *batch, int64_t hsp_capacity,
+                     int64_t *bytes);
+
+/* ---- search --------------------------------------------------------------- */
+
+/* Launch the word-hit stage of batch against db on stream (a cudaStream_t,
+ * NULL = the legacy default stream) and return at once.  Replaces H_BLAST_pre
+ * + H_BLAST (h_blast.cu:873-1157).  hsp_capacity bounds the HSP buffer (0 =
+ * runtime-options default: avg_hsps_per_sequence per subject, at least 1 Mi);
+ * if a search finds more, hbg_result_wait relaunches it once with a buffer of
+ * the exact size, so results never depend on the capacity. */
+int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt,
+               int64_t hsp_capacity, void *stream, hbg_result **out);
+
+/* Wait for the search, put HSPs in reference order -- by query, then subject,
+ * then the order the CPU word finder creates them (subject offset, then
+ * query offset) -- and copy them to the host.  Replaces H_BLAST_get_data +
+ * memory_defrag (h_blast.cu:1160-1252). */
+int hbg_result_wait(hbg_result *res);
+
+/* Device time of the word-finder kernel and of the ordering pass, in ms. */
+int hbg_result_timing(const hbg_result *res, float *wordfinder_ms, float *ordering_ms);
+
+int hbg_result_counts(const hbg_result *res, int64_t *n_hsps, int32_t *n_queries);
+
+/* Copy HSPs [first, first+count) of the ordered list. */
+int hbg_result_hsps(const hbg_result *res, int64_t first, int64_t count, hbg_hsp *out);
+
+/* Range of query q in the ordered list: HSPs [*first, *first + *count). */
+int hbg_result_query_range(const hbg_result *res, int32_t q, int64_t *first, int64_t *count);
+
+int hbg_result_stats(const hbg_result *res, int32_t q, hbg_query_stats *out);
+
+/* Release device and host buffers (replaces H_BLAST_free_memory,
+ * h_blast.cu:1254-1278). */
+int hbg_result_free(hbg_result *res);
+
+/* ---- one-call helper ------------------------------------------------------ */
+
+/* Host-to-host search: upload nothing that is already resident, run, wait and
+ * copy out.  out may be NULL to only count.  Returns HBG_ERR_CAPACITY with
+ * *n_hsps set when out_cap is too small. */
+int hbg_search_sync(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt,
+                    hbg_hsp *out, int64_t out_cap, int64_t *n_hsps,
+                    hbg_query_stats *stats, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HBLAST_GPU_H */

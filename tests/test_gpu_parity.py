@@ -1,0 +1,158 @@
+"""GPU word finder (through the C ABI) against the CPU oracle, bit-exact.
+
+Every HSP field and the per-query counters must be identical; tolerance 0
+(integer work).  Sizes are kept where the oracle finishes in seconds; the
+full-size configurations are covered by size-independent properties in
+test_gpu_properties.py.
+"""
+import numpy as np
+import pytest
+
+import hblast
+from hblast import synth
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_query(pq: hblast.ProteinQuery) -> oracle.Query:
+    return oracle.Query(pq.sequence, pq.context_offset, pq.context_length, pq.x_dropoff, pq.cutoff_score)
+
+
+def check(res: hblast.SearchResult, pqs, residues, offsets, threads=4):
+    h = res.hsps
+    # reference order: by query, subject, then (s_off, q_off)
+    key = np.lexsort((h["q_off"], h["s_off"], h["subject"], h["query"]))
+    assert np.array_equal(key, np.arange(len(h)))
+    for k, pq in enumerate(pqs):
+        ref, subj, cnt = oracle.search(oracle_query(pq), residues, offsets, nthreads=threads)
+        got = h[h["query"] == k]
+        assert len(got) == len(ref), (k, len(got), len(ref))
+        assert np.array_equal(got["subject"], subj), k
+        for f, g in (("q_start", "q_start"), ("s_start", "s_start"), ("q_off", "q_off"), ("s_off", "s_off"),
+                     ("len", "len"), ("score", "score"), ("ctx", "context")):
+            assert np.array_equal(got[g], ref[f]), (k, f)
+        st = res.stats[k]
+        assert (st["lookup_hits"], st["init_extends"], st["good_init_extends"]) == tuple(int(c) for c in cnt), k
+        assert st["subjects_passed"] == len(np.unique(subj))
+
+
+@pytest.fixture(scope="module")
+def small_db(built):
+    rng = np.random.default_rng(11)
+    qs = [synth.random_letters(rng, n) for n in (300, 57, 1200, 800, 3, 1500, 433, 96)]
+    db = synth.make_db(rng, 3000, 300, 0.6, 30, 5000, 0.05, qs, lambda r: r.integers(50, 301),
+                       lambda r: r.uniform(0.3, 0.6))
+    return qs, db, hblast.Database(db.residues, db.offsets)
+
+
+def test_plain_single_query(built):
+    qs, db = synth.plain_blastp(seed=0, n_subjects=2000)
+    gdb = hblast.Database(db.residues, db.offsets)
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs))
+    assert len(res.hsps) > 0
+    check(res, pqs, db.residues, db.offsets)
+
+
+@pytest.mark.parametrize("max_group_len", [0, 1, 4000])
+def test_batched_queries(small_db, max_group_len):
+    qs, db, gdb = small_db
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs, max_group_len=max_group_len))
+    check(res, pqs, db.residues, db.offsets)
+
+
+def test_alone_equals_in_the_mix(small_db):
+    qs, db, gdb = small_db
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    mix = hblast.search(gdb, hblast.Batch.proteins(pqs)).hsps
+    for k, pq in enumerate(pqs):
+        alone = hblast.search(gdb, hblast.Batch.proteins([pq])).hsps
+        got = mix[mix["query"] == k].copy()
+        got["query"] = 0
+        assert np.array_equal(got, alone), k
+
+
+def test_long_query_global_diagonal_table(built):
+    rng = np.random.default_rng(12)
+    q = synth.random_letters(rng, 6000)
+    db = synth.make_db(rng, 400, 300, 0.6, 30, 5000, 40, [q], lambda r: r.integers(100, 400), 0.5)
+    gdb = hblast.Database(db.residues, db.offsets)
+    pqs = [hblast.ProteinQuery.blastp(q), hblast.ProteinQuery.blastp(q[:200])]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs))
+    check(res, pqs, db.residues, db.offsets)
+
+
+def test_blastx(built):
+    rng = np.random.default_rng(13)
+    prot_q = synth.random_letters(rng, 400)
+    db = synth.make_db(rng, 600, 300, 0.6, 30, 5000, 30, [prot_q], 150, 0.6)
+    nts = synth.blastx_queries(5, db, n_queries=4)
+    xd = np.full((4, 6), 16, dtype=np.int32)
+    cu = np.full((4, 6), 41, dtype=np.int32)
+    cu[1] = [30, 35, 41, 41, 38, 33]
+    gdb = hblast.Database(db.residues, db.offsets)
+    res = hblast.search(gdb, hblast.Batch.blastx(nts, xd, cu))
+    pqs = []
+    for k, nt in enumerate(nts):
+        prot, off, ln = oracle.translate6(nt)
+        pqs.append(hblast.ProteinQuery(prot, off, ln, xd[k], cu[k]))
+    assert len(res.hsps) > 0
+    check(res, pqs, db.residues, db.offsets)
+
+
+def test_edge_subjects(built):
+    rng = np.random.default_rng(14)
+    q = synth.random_letters(rng, 120)
+    subs = [np.zeros(0, np.uint8), q[:1], q[:2], q[:3], q[:4], q.copy(), np.concatenate([q, q, q]),
+            np.full(200, 1, np.uint8), np.full(300, 20, np.uint8), np.array(list(range(1, 28)) * 10, np.uint8),
+            synth.random_letters(rng, 40000)]
+    lens = [len(s) for s in subs]
+    offsets = np.zeros(len(subs) + 1, np.int64)
+    offsets[1:] = np.cumsum(lens)
+    residues = np.concatenate(subs).astype(np.uint8)
+    gdb = hblast.Database(residues, offsets)
+    pqs = [hblast.ProteinQuery.blastp(q), hblast.ProteinQuery.blastp(np.full(50, 1, np.uint8), 16, 20),
+           hblast.ProteinQuery.blastp(np.full(64, 20, np.uint8), 10, 30)]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs))
+    check(res, pqs, residues, offsets)
+
+
+def test_empty_database(built):
+    gdb = hblast.Database(np.zeros(0, np.uint8), np.zeros(1, np.int64))
+    res = hblast.search(gdb, hblast.Batch.proteins([hblast.ProteinQuery.blastp(np.ones(50, np.uint8))]))
+    assert len(res.hsps) == 0 and res.stats[0]["lookup_hits"] == 0
+
+
+def test_capacity_overflow_relaunch(small_db):
+    qs, db, gdb = small_db
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs[:3]]
+    batch = hblast.Batch.proteins(pqs)
+    full = hblast.search(gdb, batch)
+    tiny = hblast.search(gdb, batch, hsp_capacity=1)
+    assert len(full.hsps) > 1
+    assert np.array_equal(full.hsps, tiny.hsps)
+
+
+def test_smallbone_table(built):
+    from test_host import smallbone_from_csr
+    rng = np.random.default_rng(15)
+    q = synth.random_letters(rng, 350)
+    db = synth.make_db(rng, 500, 300, 0.6, 30, 5000, 25, [q], 120, 0.45)
+    cs, oe = oracle.lookup_table(oracle.Query.blastp(q), 11)
+    cells, overflow = smallbone_from_csr(cs, oe)
+    gdb = hblast.Database(db.residues, db.offsets)
+    pq = hblast.ProteinQuery.blastp(q)
+    res = hblast.search(gdb, hblast.Batch.from_smallbone(pq, cells, overflow))
+    check(res, [pq], db.residues, db.offsets)
+
+
+def test_launch_shapes_do_not_change_results(small_db):
+    qs, db, gdb = small_db
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    batch = hblast.Batch.proteins(pqs)
+    base = hblast.search(gdb, batch).hsps
+    for threads, blocks in ((32, 1), (64, 7), (256, 1000)):
+        o = hblast.default_options(num_threadsx=threads, num_blocksx=blocks)
+        assert np.array_equal(hblast.search(gdb, batch, options=o).hsps, base), (threads, blocks)

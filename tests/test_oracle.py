@@ -1,0 +1,158 @@
+"""The CPU oracle against the reference's tables and hand-derived known answers.
+
+The reference ships no golden vectors for this path, so the oracle is pinned
+by (1) the BLOSUM62 table and constants extracted from the H-BLAST sources
+(tests/golden/reference_tables.json, made by tests/golden/make_golden.py) and
+(2) cases whose expected HSPs are worked out by hand below from the published
+NCBI two-hit algorithm (H-BLAST restates it at h_blast_kernel.cu:672-871 and
+1069-1540).
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+GOLD = json.loads((Path(__file__).parent / "golden" / "reference_tables.json").read_text())
+L = "-ABCDEFGHIKLMNPQRSTVWXYZU*OJ"
+
+
+def enc(s: str) -> np.ndarray:
+    return np.array([L.index(c) for c in s], dtype=np.uint8)
+
+
+def hand_lut(cells: dict):
+    """CSR lookup table from {word string: [query offsets]}."""
+    cs = np.zeros(oracle.NCELLS + 1, dtype=np.int32)
+    items = {}
+    for w, offs in cells.items():
+        a, b, c = enc(w)
+        items[(int(a) << 10) | (int(b) << 5) | int(c)] = sorted(offs)
+    ent = []
+    for i in range(oracle.NCELLS):
+        cs[i] = len(ent)
+        ent += items.get(i, [])
+    cs[oracle.NCELLS] = len(ent)
+    return cs, np.array(ent or [0], dtype=np.int32)[:len(ent)]
+
+
+def run(q: str, s: str, cells: dict, xdrop=16, cutoff=30):
+    query = oracle.Query.blastp(enc(q), xdrop, cutoff)
+    sub = enc(s)
+    off = np.array([0, len(sub)], dtype=np.int64)
+    h, subj, cnt = oracle.search(query, sub, off, lut=hand_lut(cells))
+    rows = [tuple(int(x) for x in r) for r in h]
+    return rows, [int(c) for c in cnt]
+
+
+def test_matrix_matches_reference(built):
+    m = np.array(GOLD["blosum62_ncbistdaa_28x32"])
+    for a in range(28):
+        for b in range(28):
+            assert oracle.score(a, b) == m[a, b], (a, b)
+    assert (m[:, 28:] == -128).all()
+    assert (m[0] == -128).all() and (m[:, 0] == -128).all()
+
+
+def test_product_matrix_matches_reference(built):
+    from hblast import synth
+    m = np.array(GOLD["blosum62_ncbistdaa_28x32"])
+    assert np.array_equal(synth.blosum62(), m[:, :28])
+    assert (m[:28, :28] == m[:28, :28].T).all()   # symmetric: [q][s] and [s][q] agree
+
+
+def test_reference_constants():
+    assert GOLD["charsize"] == 5            # 5 bits per letter -> 32768 cells
+    assert GOLD["aa_hits_per_cell"] == 3    # smallbone cells hold 3 offsets inline
+
+
+def test_two_hits_on_runs(built):
+    # Q = S = A x 10 (A/A = 4); cell AAA = {0, 5}.  Diagonals 0, -1, -2 get a
+    # second hit at s = 5, 6, 7 (diff 5).  At s=5: word end q_r = s_r = 8,
+    # left walk over 8 letters scores 32 (left_d 8 >= 8-3), right walk 2 more
+    # letters -> len 10, score 40.  At s=6: q_r=8, s_r=9, left 8 letters (32),
+    # right 1 letter -> s_start 1, len 9, score 36.  At s=7: s_r=10 = end,
+    # left 8 letters, no right letters -> s_start 2, len 8, score 32.
+    rows, cnt = run("A" * 10, "A" * 10, {"AAA": [0, 5]})
+    assert rows == [(0, 0, 5, 5, 10, 40, 0), (0, 1, 5, 6, 9, 36, 0), (0, 2, 5, 7, 8, 32, 0)]
+    assert cnt == [16, 3, 3]
+
+
+@pytest.mark.parametrize("D,extended", [(2, 0), (3, 1), (39, 1), (40, 0), (41, 0)])
+def test_window_boundaries(built, D, extended):
+    # Hits (0,0) and (D,D) on diagonal 0: extend only when 3 <= D < 40.
+    if D < 3:
+        q = "W" * (D + 3) + "G" * 10
+        s = "W" * (D + 3) + "P" * 10
+    else:
+        q = "WWW" + "G" * (D - 3) + "WWW" + "G" * 10
+        s = "WWW" + "P" * (D - 3) + "WWW" + "P" * 10
+    rows, cnt = run(q, s, {"WWW": [0, D]}, cutoff=41)
+    assert cnt[1] == extended
+    if D == 39:
+        # word at 39..41 scores 33 (right_d 3); the left walk keeps only
+        # those three letters (G/P = -2 drops 16 after 8 letters), so
+        # left_d 3 < 42 - 3: no right walk; score 33 < 41 -> not kept.
+        assert rows == [] and cnt[2] == 0
+
+
+def test_three_apart_extends_and_sets_flag(built):
+    # Q = W x 6 + G x 10, S = W x 6 + P x 10, cell WWW = {0, 3}: diagonal 0
+    # has hits at s=0 and s=3 (diff 3).  q_r = s_r = 6, left walk 6 W/W = 66,
+    # right walk: G/P = -2 per letter, stops after 8 letters (drop 16) with
+    # no gain -> HSP (0, 0, len 6, score 66).
+    rows, cnt = run("W" * 6 + "G" * 10, "W" * 6 + "P" * 10, {"WWW": [0, 3]}, cutoff=41)
+    assert rows == [(0, 0, 3, 3, 6, 66, 0)]
+    assert cnt == [8, 1, 1]
+
+
+def test_flag_suppresses_hits_inside_extension(built):
+    # Same extension as above (every letter of S[6..15] scores -2 against G),
+    # so the right walk ends at s_last_off = 13 and diagonal 0 is flagged with
+    # last = 11.  The only other hits are EHK at q=s=8 (inside the extended
+    # region: skipped; without the flag it would be a second extension at
+    # diff 5) and QRT at q=s=12 (>= 11: resets the diagonal, no extension).
+    q = "W" * 6 + "G" * 10
+    s = "W" * 6 + "PPEHKPQRTP"
+    rows, cnt = run(q, s, {"WWW": [0, 3], "EHK": [8], "QRT": [12]}, cutoff=41)
+    assert rows == [(0, 0, 3, 3, 6, 66, 0)]
+    assert cnt == [10, 1, 1]
+
+
+def test_translation_known_codons(built):
+    # ATG GCC TAA -> M A *; the reverse complement TTA GGC CAT -> L G H.
+    nt = np.array([0, 3, 2, 2, 1, 1, 3, 0, 0], dtype=np.uint8)   # A T G G C C T A A
+    prot, off, ln = oracle.translate6(nt)
+    frames = [prot[o:o + n] for o, n in zip(off, ln)]
+    assert list(ln) == [3, 2, 2, 3, 2, 2]
+    assert "".join(L[x] for x in frames[0]) == "MA*"
+    assert "".join(L[x] for x in frames[3]) == "LGH"
+    assert all(prot[o - 1] == 0 for o in off[1:])   # one sentinel between frames
+
+
+def test_lookup_table_rule(built):
+    rng = np.random.default_rng(3)
+    q = rng.integers(1, 23, size=40).astype(np.uint8)
+    cs, ent = oracle.lookup_table(oracle.Query.blastp(q), 11)
+    m = np.array(GOLD["blosum62_ncbistdaa_28x32"])[:, :28]
+    # every stored (word, offset) scores >= 11 and every word >= 11 is stored
+    for w in rng.integers(0, 32768, size=3000):
+        a, b, c = w >> 10, (w >> 5) & 31, w & 31
+        stored = set(ent[cs[w]:cs[w + 1]].tolist())
+        assert list(ent[cs[w]:cs[w + 1]]) == sorted(stored)
+        for p in range(len(q) - 2):
+            ok = a < 28 and b < 28 and c < 28 and m[q[p], a] + m[q[p + 1], b] + m[q[p + 2], c] >= 11
+            assert (p in stored) == bool(ok)
+
+
+def test_threads_do_not_change_results(built):
+    from hblast import synth
+    rng = np.random.default_rng(5)
+    q = synth.random_letters(rng, 200)
+    db = synth.make_db(rng, 300, 300, 0.6, 30, 5000, 30, [q], 100, 0.5)
+    a = oracle.search(oracle.Query.blastp(q), db.residues, db.offsets, nthreads=1)
+    b = oracle.search(oracle.Query.blastp(q), db.residues, db.offsets, nthreads=4)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert len(a[0]) > 0
