@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark of the BLASTP word-hit stage on the batched workload.
+
+Workload (default, --config batched): 64 protein queries of 50..1500 aa against
+2,000,000 lognormal subjects (~720 M uint8 residues resident in HBM), word 3,
+T=11, window 40, X-drop 16, cutoff 41, seed 0.  One step = one search of the
+whole batch against the whole database (seed scan + two-hit + ungapped
+extension + ordering pass).  Metric: query x db residues per second,
+sum(query lengths) * sum(subject lengths) / step time.
+
+Arms:
+  default            the GB300 path through the C ABI; prints one JSON line.
+  --impl reference   the reference's CPU word finder on the host cores: the C
+                     restatement in oracle/ (the H-BLAST/NCBI sources cannot be
+                     built here), all host threads, on a bounded sample of the
+                     same workload.
+
+Multi-GPU (torchrun, N > 1): subjects shard across ranks with no collective on
+the data path; each rank searches its own database of the configured size
+(weak scaling) and the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "h-blast_gb300"))
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "query x db residues/s"
+UNIT = "residues/s"
+HSP_BYTES = 36
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="hblast", choices=["hblast", "reference"])
+    p.add_argument("--config", default="batched", choices=["batched", "plain"])
+    p.add_argument("--subjects", type=int, default=0, help="override the database size (testing)")
+    p.add_argument("--queries", type=int, default=0, help="override the number of queries (testing)")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true", help="skip the one-query-per-launch comparison")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# --------------------------------------------------------------------------- workload
+
+def workload(cfg: str, rank: int, n_subjects: int, n_queries: int):
+    from hblast import synth
+    if cfg == "plain":
+        qs, db = synth.plain_blastp(seed=rank, n_subjects=n_subjects or 20000)
+        desc = dict(workload="plain blastp: 1 query of 300 aa vs 20,000 lognormal subjects (median 300, "
+                             "sigma 0.6, 30..5000), 50 planted 120-aa segments at 40% identity")
+    else:
+        qs, db = synth.batched_blastp(seed=rank, n_queries=n_queries or 64, n_subjects=n_subjects or 2_000_000)
+        desc = dict(workload="batched blastp: 64 queries of 50..1500 aa vs 2,000,000 lognormal subjects "
+                             "(median 300, sigma 0.6, 30..5000), 1% planted 50..300 aa at 30..60% identity")
+    return qs, db, desc
+
+
+# --------------------------------------------------------------------------- clocks
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons, pw = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                pw.append(float(r[3]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(pw) if pw else None}
+
+
+# --------------------------------------------------------------------------- CPU sides
+
+def cpu_sample_search(qs, db, seconds: float, threads: int):
+    """Run the oracle over a prefix of the subjects sized to ~`seconds`;
+    returns (query x db residues/s, seconds, subjects used, residues used)."""
+    from oracle import oracle
+    luts = [oracle.lookup_table(oracle.Query.blastp(q), 11) for q in qs]
+    oq = [oracle.Query.blastp(q) for q in qs]
+    qsum = float(sum(len(q) for q in qs))
+
+    def run(n):
+        t0 = time.perf_counter()
+        for q, lut in zip(oq, luts):
+            oracle.search(q, db.residues, db.offsets, nthreads=threads, subj_range=(0, n), lut=lut)
+        return time.perf_counter() - t0
+
+    n = min(db.n, 2000)
+    t = run(n)
+    while t < seconds / 4 and n < db.n:
+        n = min(db.n, int(n * max(2.0, seconds / max(t, 1e-3) * 0.9)))
+        t = run(n)
+    res = float(db.offsets[n] - db.offsets[0])
+    return qsum * res / t, t, n, int(res)
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import __graft_entry__ as g
+    from oracle import oracle
+    oracle.build()
+    _ = g  # the reference arm runs only the CPU restatement
+    qs, db, desc = workload(args.config, 0, args.subjects, args.queries)
+    threads = os.cpu_count() or 1
+    # size one step to ~4 s so that warmup + steps end within a few minutes
+    _, _, n, res = cpu_sample_search(qs, db, 4.0, threads)
+    from oracle import oracle as orc
+    luts = [orc.lookup_table(orc.Query.blastp(q), 11) for q in qs]
+    oq = [orc.Query.blastp(q) for q in qs]
+    qsum = sum(len(q) for q in qs)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for q, lut in zip(oq, luts):
+            orc.search(q, db.residues, db.offsets, nthreads=threads, subj_range=(0, n), lut=lut)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = sum(times) / len(times)
+    value = qsum * res / t
+    sample = f"{len(qs)} queries x first {n} subjects ({res} residues) of the workload per step"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": dict(desc, sample=sample),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "what": "C restatement of the NCBI BLAST+ 2.2.28 two-hit word finder (oracle/)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# --------------------------------------------------------------------------- GPU arm
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    import __graft_entry__ as g
+    g.build()
+    import hblast
+
+    qs, db, desc = workload(args.config, rank, args.subjects, args.queries)
+    qsum = int(sum(len(q) for q in qs))
+    ssum = int(db.offsets[-1])
+    units_per_step = float(qsum) * float(ssum)
+    opts = hblast.default_options(method=0)
+    gdb = hblast.Database(db.residues, db.offsets, opts)
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    batch = hblast.Batch.proteins(pqs)
+    binfo = batch.info()
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+
+    # warm-up (also sizes the HSP buffer so that no timed step relaunches)
+    s = hblast.Searcher(gdb, batch, opts)
+    for _ in range(max(args.warmup, 1)):
+        s.launch(sptr)
+        s.sync()
+    n_hsps = s.n_hsps()
+    s.close()
+    s = hblast.Searcher(gdb, batch, opts, hsp_capacity=max(int(n_hsps * 1.1) + 1024, 1 << 20))
+    for _ in range(args.warmup):
+        s.launch(sptr)
+        s.sync()
+
+    # timed region: device-resident inputs, events on the launching stream
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    wf_ms, ord_ms = [], []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        s.launch(sptr)
+        s.sync()
+        a, b, launches = s.timing()
+        wf_ms.append(a)
+        ord_ms.append(b)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+        dist.barrier()
+    value = units_per_step * args.steps * world / elapsed
+    ms_step = elapsed / args.steps * 1e3
+    s.wait()
+    res = s.result()
+    n_hsps = len(res.hsps)
+    stats = res.stats
+    hits = sum(st["lookup_hits"] for st in stats)
+    ext = sum(st["init_extends"] for st in stats)
+    s.close()
+
+    # roofline of the word-finder kernel (HBM-bound subject stream)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    wf_avg = sum(wf_ms) / len(wf_ms) / 1e3
+    alg_bytes = ssum + 8 * db.n + HSP_BYTES * n_hsps
+    achieved = alg_bytes / wf_avg / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "wordfinder_traffic.json"
+    if tfile.exists():
+        try:
+            tj = json.loads(tfile.read_text())
+            if tj.get("config") == args.config:
+                traffic = tj.get("dram_bytes_per_launch")
+        except ValueError:
+            pass
+
+    # one-query-per-launch form (the plain GPU form) on the same database
+    plain = None
+    if not args.no_plain and args.config == "batched":
+        single = [hblast.Batch.proteins([p]) for p in pqs]
+        sss = [hblast.Searcher(gdb, b1, opts) for b1 in single]
+        for x in sss:
+            x.launch(sptr)
+            x.sync()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            for x in sss:
+                x.launch(sptr)
+                x.sync()
+        torch.cuda.synchronize()
+        tp = (time.perf_counter() - t0) / reps
+        plain = {"value": units_per_step * world / tp, "unit": UNIT, "ms_per_step": tp * 1e3,
+                 "form": "64 launches, one query each, same database"}
+        for x in sss:
+            x.close()
+        for b1 in single:
+            b1.close()
+
+    # end to end through the public API: host queries in, ordered HSPs out
+    e2e = None
+    if not args.no_e2e:
+        times = []
+        h2d = d2h = 0
+        for i in range(1 + max(1, args.steps // 3)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b2 = hblast.Batch.proteins(pqs)
+            r2 = hblast.search(gdb, b2, opts, hsp_capacity=max(int(n_hsps * 1.1) + 1024, 1 << 20), stream=sptr)
+            h2d = b2.info()["device_bytes"]
+            b2.close()
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(time.perf_counter() - t0)
+            d2h = HSP_BYTES * len(r2.hsps) + 8 * (1 + 4 * len(pqs))
+        te = sum(times) / len(times)
+        e2e = {"value": units_per_step * world / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": te * 1e3,
+               "path": "hbg_batch_create (host lookup tables) + hbg_search + hbg_result_wait"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, t, n, r = cpu_sample_search(qs, db, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{len(qs)} queries x first {n} subjects ({r} residues), {t:.1f} s",
+               "what": "C restatement of the NCBI BLAST+ 2.2.28 two-hit word finder (oracle/)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded; BLOSUM62-implied background)",
+            "config": dict(desc, queries=len(qs), query_residues=qsum, subjects=db.n, subject_residues=ssum,
+                           groups=binfo["n_groups"], l2="inputs larger than L2 (database > 129 MB)",
+                           parallelism=f"replicas x{world}, subjects sharded per rank (no collective)"),
+            "gpu_launches": int(launches) * args.steps,
+            "clocks": ck,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "kernel": "wordfinder_kernel", "kernel_ms": wf_avg * 1e3,
+                         "algorithmic_bytes": int(alg_bytes)},
+            "lookup_hits_per_s": hits / wf_avg, "extensions_per_s": ext / wf_avg,
+            "hsps": n_hsps, "ordering_ms": sum(ord_ms) / len(ord_ms),
+            "e2e": e2e, "plain": plain,
+            "batched_over_plain": (value / plain["value"]) if plain else None,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

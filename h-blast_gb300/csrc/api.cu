@@ -131,11 +131,18 @@ struct hbg_result {
     std::vector<hbg_query_stats> stats;
     std::vector<int64_t> q_first, q_count;
     int64_t n_hsps = 0;
-    bool launched = false, done = false;
+    bool launched = false, synced = false, done = false;
     float wf_ms = 0.f, ord_ms = 0.f;
+    int32_t launches = 0;   // kernels per search
 };
 
 namespace {
+
+int64_t batch_device_bytes(const hbg::HostBatch &h) {
+    return (int64_t)(h.groups.size() * sizeof(HbgGroup) + h.contexts.size() * sizeof(HbgContext) +
+                     h.queries.size() * sizeof(HbgQueryDesc) + h.letters.size() + h.ctx_of.size() * 4 +
+                     h.cells.size() * 4 + h.entries.size() * 2 + h.pv.size() * 4 + h.query_cells.size() * 2);
+}
 
 int upload_batch(hbg_batch *b, int device) {
     if (b->device == device)
@@ -164,10 +171,7 @@ int upload_batch(hbg_batch *b, int device) {
         CU(cudaMemcpy(b->d_entries, h.entries.data(), h.entries.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_pv, h.pv.data(), h.pv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_qcells, h.query_cells.data(), h.query_cells.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
-    b->device_bytes = (int64_t)(h.groups.size() * sizeof(HbgGroup) + h.contexts.size() * sizeof(HbgContext) +
-                                h.queries.size() * sizeof(HbgQueryDesc) + h.letters.size() +
-                                h.ctx_of.size() * 4 + h.cells.size() * 4 + h.entries.size() * 2 +
-                                h.pv.size() * 4 + h.query_cells.size() * 2);
+    b->device_bytes = batch_device_bytes(h);
     b->device = device;
     return HBG_OK;
 }
@@ -294,11 +298,17 @@ int launch_search(hbg_result *r) {
     if (o.bits_q + o.bits_s + o.bits_so + o.bits_qo > 64)
         return fail(HBG_ERR_TOO_LONG, "ordering key exceeds 64 bits for this database and batch");
     CU(hbg::launch_order(o, st));
+    {
+        const int bits = o.bits_q + o.bits_s + o.bits_so + o.bits_qo;
+        r->launches = (db->n > 0 ? 1 : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 2 + 3 * ((bits + 7) / 8) : 0) +
+                      (nq > 0 ? 1 : 0);
+    }
     CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
     CU(cudaEventRecord(r->ev[2], st));
     CU(cudaMemcpyAsync(r->h_counters, r->d_counters, r->n_counters * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, st));
     r->launched = true;
+    r->synced = false;
     r->done = false;
     return HBG_OK;
 }
@@ -638,7 +648,8 @@ int hbg_batch_destroy(hbg_batch *b) {
     return HBG_OK;
 }
 
-int hbg_batch_info(const hbg_batch *b, int32_t *nq, int32_t *ng, int64_t *qlen, int64_t *entries) {
+int hbg_batch_info(const hbg_batch *b, int32_t *nq, int32_t *ng, int64_t *qlen, int64_t *entries,
+                   int64_t *device_bytes) {
     if (!b)
         return fail(HBG_ERR_INVALID, "null batch");
     if (nq)
@@ -653,6 +664,8 @@ int hbg_batch_info(const hbg_batch *b, int32_t *nq, int32_t *ng, int64_t *qlen, 
     }
     if (entries)
         *entries = (int64_t)b->host.entries.size();
+    if (device_bytes)
+        *device_bytes = batch_device_bytes(b->host);
     return HBG_OK;
 }
 
@@ -660,7 +673,7 @@ int hbg_mem_required(const hbg_db *db, const hbg_batch *b, int64_t cap, int64_t 
     if (!db || !b || !bytes || cap < 0)
         return fail(HBG_ERR_INVALID, "hbg_mem_required: bad argument");
     if (cap == 0)
-        cap = std::max<int64_t>(1 << 20, (int64_t)db->n * 20);
+        cap = std::max<int64_t>(1 << 20, (int64_t)db->n);
     const hbg::HostBatch &h = b->host;
     int64_t batch_bytes = (int64_t)(h.letters.size() + h.ctx_of.size() * 4 + h.cells.size() * 4 +
                                     h.entries.size() * 2 + h.pv.size() * 4 + h.query_cells.size() * 2);
@@ -721,7 +734,7 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
         r->blocks = sms * per;
     }
     if (cap == 0)
-        cap = std::max<int64_t>(1 << 20, (int64_t)db->n * 20);
+        cap = std::max<int64_t>(1 << 20, (int64_t)db->n);
     rc = prepare_result(r, std::max<int64_t>(cap, r->cap));
     if (rc == HBG_OK)
         rc = launch_search(r);
@@ -736,10 +749,10 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
     return HBG_OK;
 }
 
-int hbg_result_wait(hbg_result *r) {
+int hbg_result_sync(hbg_result *r) {
     if (!r || !r->launched)
         return fail(HBG_ERR_STATE, "no search launched on this result");
-    if (r->done)
+    if (r->synced)
         return HBG_OK;
     DeviceScope ds(r->device);
     CU(cudaStreamSynchronize(r->stream));
@@ -760,6 +773,18 @@ int hbg_result_wait(hbg_result *r) {
     r->n_hsps = (int64_t)n;
     CU(cudaEventElapsedTime(&r->wf_ms, r->ev[0], r->ev[1]));
     CU(cudaEventElapsedTime(&r->ord_ms, r->ev[1], r->ev[2]));
+    r->synced = true;
+    return HBG_OK;
+}
+
+int hbg_result_wait(hbg_result *r) {
+    int rc = hbg_result_sync(r);
+    if (rc != HBG_OK)
+        return rc;
+    if (r->done)
+        return HBG_OK;
+    DeviceScope ds(r->device);
+    const int64_t n = r->n_hsps;
     r->hsps.resize((size_t)n);
     if (n)
         CU(cudaMemcpy(r->hsps.data(), r->d_sorted, (size_t)n * sizeof(hbg_hsp), cudaMemcpyDeviceToHost));
@@ -785,18 +810,20 @@ int hbg_result_wait(hbg_result *r) {
     return HBG_OK;
 }
 
-int hbg_result_timing(const hbg_result *r, float *wf, float *ord) {
-    if (!r || !r->done)
+int hbg_result_timing(const hbg_result *r, float *wf, float *ord, int32_t *launches) {
+    if (!r || !r->synced)
         return fail(HBG_ERR_STATE, "result not collected");
     if (wf)
         *wf = r->wf_ms;
     if (ord)
         *ord = r->ord_ms;
+    if (launches)
+        *launches = r->launches;
     return HBG_OK;
 }
 
 int hbg_result_counts(const hbg_result *r, int64_t *n_hsps, int32_t *n_queries) {
-    if (!r || !r->done)
+    if (!r || !r->synced)
         return fail(HBG_ERR_STATE, "result not collected");
     if (n_hsps)
         *n_hsps = r->n_hsps;
@@ -838,7 +865,7 @@ int hbg_result_free(hbg_result *r) {
     if (!r)
         return fail(HBG_ERR_INVALID, "null result");
     DeviceScope ds(r->device);
-    if (r->launched && !r->done)
+    if (r->launched && !r->synced)
         cudaStreamSynchronize(r->stream);
     free_result_device(r);
     delete r;

@@ -80,11 +80,12 @@ _SIGS = {
                                 C.POINTER(C.c_int32), _P], C.c_int),
     "hbg_batch_destroy": ([_P], C.c_int),
     "hbg_batch_info": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
-                        C.POINTER(C.c_int64)], C.c_int),
+                        C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
     "hbg_mem_required": ([_P, _P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     "hbg_search": ([_P, _P, C.POINTER(GpuOptions), C.c_int64, _P, C.POINTER(_P)], C.c_int),
     "hbg_result_wait": ([_P], C.c_int),
-    "hbg_result_timing": ([_P, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
+    "hbg_result_sync": ([_P], C.c_int),
+    "hbg_result_timing": ([_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int32)], C.c_int),
     "hbg_result_counts": ([_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)], C.c_int),
     "hbg_result_hsps": ([_P, C.c_int64, C.c_int64, _P], C.c_int),
     "hbg_result_query_range": ([_P, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
@@ -256,9 +257,10 @@ class Batch:
         return cls(h, 1)
 
     def info(self):
-        nq, ng, ql, ne = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64()
-        _check(lib().hbg_batch_info(self.handle, C.byref(nq), C.byref(ng), C.byref(ql), C.byref(ne)))
-        return dict(n_queries=nq.value, n_groups=ng.value, total_query_len=ql.value, lookup_entries=ne.value)
+        nq, ng, ql, ne, db = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().hbg_batch_info(self.handle, C.byref(nq), C.byref(ng), C.byref(ql), C.byref(ne), C.byref(db)))
+        return dict(n_queries=nq.value, n_groups=ng.value, total_query_len=ql.value, lookup_entries=ne.value,
+                    device_bytes=db.value)
 
     def lookup_table(self, g: int):
         """(cells[32769] uint32, entries uint16, first_query, query_starts) of group g."""
@@ -310,7 +312,12 @@ class Searcher:
                                 C.c_void_p(stream) if stream else None, C.byref(self.res)))
 
     def wait(self) -> None:
+        """Wait, order and copy the HSPs to the host."""
         _check(lib().hbg_result_wait(self.res))
+
+    def sync(self) -> None:
+        """Wait for the device work only (HSPs stay in device memory)."""
+        _check(lib().hbg_result_sync(self.res))
 
     def n_hsps(self) -> int:
         n, q = C.c_int64(), C.c_int32()
@@ -318,9 +325,10 @@ class Searcher:
         return n.value
 
     def timing(self):
-        a, b = C.c_float(), C.c_float()
-        _check(lib().hbg_result_timing(self.res, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(word-finder ms, ordering ms, kernels launched per search)."""
+        a, b, n = C.c_float(), C.c_float(), C.c_int32()
+        _check(lib().hbg_result_timing(self.res, C.byref(a), C.byref(b), C.byref(n)))
+        return a.value, b.value, n.value
 
     def result(self) -> SearchResult:
         n = self.n_hsps()
@@ -333,7 +341,7 @@ class Searcher:
             _check(lib().hbg_result_stats(self.res, q, C.byref(s)))
             stats.append(dict(lookup_hits=s.lookup_hits, init_extends=s.init_extends,
                               good_init_extends=s.good_init_extends, subjects_passed=s.subjects_passed))
-        wf, od = self.timing()
+        wf, od, _ = self.timing()
         return SearchResult(out, stats, wf, od)
 
     def query_range(self, q: int):

@@ -205,8 +205,9 @@ int hbg_batch_lookup_table(const hbg_batch *batch, int32_t g, uint32_t *cells,
                            int32_t *first_query, int32_t *n_queries, int32_t *query_start);
 
 int hbg_batch_destroy(hbg_batch *batch);
+/* Sizes of a batch; device_bytes is what its upload copies host-to-device. */
 int hbg_batch_info(const hbg_batch *batch, int32_t *n_queries, int32_t *n_groups,
-                   int64_t *total_query_len, int64_t *lookup_entries);
+                   int64_t *total_query_len, int64_t *lookup_entries, int64_t *device_bytes);
 
 /* Estimate of the device bytes one search of batch against db needs beyond
  * the resident database (replaces H_BLAST_check_memory, h_blast.cu:1280-1349).
@@ -219,7 +220,8 @@ int hbg_mem_required(const hbg_db *db, const hbg_batch *batch, int64_t hsp_capac
 /* Launch the word-hit stage of batch against db on stream (a cudaStream_t,
  * NULL = the legacy default stream) and return at once.  Replaces H_BLAST_pre
  * + H_BLAST (h_blast.cu:873-1157).  hsp_capacity bounds the HSP buffer (0 =
- * runtime-options default: avg_hsps_per_sequence per subject, at least 1 Mi);
+ * one slot per subject, at least 1 Mi; H-BLAST sizes it as AVG_HSPS_PER_SEQUENCE
+ * slots per subject, NF/functions.cpp:1513-1516);
  * if a search finds more, hbg_result_wait relaunches it once with a buffer of
  * the exact size, so results never depend on the capacity. */
 int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt,
@@ -231,8 +233,16 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt,
  * memory_defrag (h_blast.cu:1160-1252). */
 int hbg_result_wait(hbg_result *res);
 
-/* Device time of the word-finder kernel and of the ordering pass, in ms. */
-int hbg_result_timing(const hbg_result *res, float *wordfinder_ms, float *ordering_ms);
+/* Wait for the search and read its counters and timings without copying the
+ * HSPs to the host (they stay ordered in device memory); hbg_result_wait may
+ * follow to copy them.  Relaunches on HSP-buffer overflow like
+ * hbg_result_wait. */
+int hbg_result_sync(hbg_result *res);
+
+/* Device time of the word-finder kernel and of the ordering pass, in ms,
+ * and the number of kernels one search launches. */
+int hbg_result_timing(const hbg_result *res, float *wordfinder_ms, float *ordering_ms,
+                      int32_t *kernel_launches);
 
 int hbg_result_counts(const hbg_result *res, int64_t *n_hsps, int32_t *n_queries);
 
