@@ -36,7 +36,7 @@ constexpr int kSmemDiag = 2048;   // must equal kSmemDiagLen in batch_builder.h
 constexpr int kMaxQ = 64;         // kMaxQueriesPerGroup
 constexpr uint32_t kFlag = 0x80000000u;
 constexpr uint32_t kLast = 0x7fffffffu;
-constexpr int32_t kWrap = 1 << 30;
+constexpr int32_t kWrap = 1 << 29;  // offset + subject length stays below 2^31 - 1
 
 __constant__ int8_t c_blosum[28 * 32] = {
 #include "blosum62.inc"
@@ -141,6 +141,151 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
     return r;
 }
+// ---------------------------------------------------------------------------
+// Per-warp state.  Extensions are queued and run one lane per extension; the
+// diagonal of a queued extension holds a "pending" marker (flag bit + the
+// current offset - 1, a value no real state of this subject can take, and one
+// that reads as a stale, already-passed flag once the offset moves on), and a
+// later hit that meets the marker is parked in the blocked list, in order,
+// until the extension has written the diagonal's real state.
+
+constexpr int kQueue = 64;
+
+struct WarpQueue {
+    int task_s[kQueue];      // subject offset of the second hit
+    int task_q[kQueue];      // group-local query offset
+    int task_left[kQueue];   // one past the first hit's word (subject offset)
+    int blk_s[2][kQueue];
+    int blk_q[2][kQueue];
+};
+
+struct Item {
+    const uint8_t *s;        // subject letters
+    int S;                   // subject length
+    int j;                   // subject ordinal id
+    uint32_t *diag;
+    int mask;
+    int dofs;                // NCBI diagonal offset for this subject
+    int window;
+    const uint8_t *gseq;
+    const int32_t *gctx;
+    int first_query;
+};
+
+// Apply one batch of hits (one per active lane, in CPU order by lane) to the
+// diagonal table.  Lanes sharing a diagonal go in lane order.  Warp-collective.
+__device__ __forceinline__ void apply_hits(const Item &it, bool act, int d, int s_h, int q,
+                                           WarpQueue &wq, int &n_tasks, int &n_blk, int blk_out) {
+    const unsigned am = __ballot_sync(0xffffffffu, act);
+    int rank = 0;
+    if (act) {
+        const unsigned grp = __match_any_sync(am, d);
+        rank = __popc(grp & lanemask_lt());
+    }
+    bool pending = act;
+    const uint32_t pend = kFlag | (uint32_t)(it.dofs - 1);
+    for (int rr = 0;; ++rr) {
+        bool want_task = false, want_blk = false;
+        int left = 0;
+        if (pending && rank == rr) {
+            pending = false;
+            const uint32_t cell = it.diag[d];
+            if (cell == pend) {
+                want_blk = true;
+            } else if (cell & kFlag) {
+                if (s_h + it.dofs >= (int32_t)(cell & kLast))
+                    it.diag[d] = (uint32_t)(s_h + it.dofs);
+            } else {
+                const int32_t last = (int32_t)cell - it.dofs;   // subject offset of the last hit
+                const int32_t diff = s_h - last;
+                if (diff >= it.window) {
+                    it.diag[d] = (uint32_t)(s_h + it.dofs);
+                } else if (diff >= 3) {
+                    want_task = true;
+                    left = last + 3;
+                    it.diag[d] = pend;
+                }
+            }
+        }
+        const unsigned tm = __ballot_sync(0xffffffffu, want_task);
+        if (want_task) {
+            const int p = n_tasks + __popc(tm & lanemask_lt());
+            wq.task_s[p] = s_h;
+            wq.task_q[p] = q;
+            wq.task_left[p] = left;
+        }
+        n_tasks += __popc(tm);
+        const unsigned bm = __ballot_sync(0xffffffffu, want_blk);
+        if (want_blk) {
+            const int p = n_blk + __popc(bm & lanemask_lt());
+            wq.blk_s[blk_out][p] = s_h;
+            wq.blk_q[blk_out][p] = q;
+        }
+        n_blk += __popc(bm);
+        __syncwarp();
+        if (!__any_sync(0xffffffffu, pending))
+            break;
+    }
+}
+
+// Run every queued extension (lane per extension), then replay the blocked
+// hits in order, until neither list has work.  Warp-collective.
+__device__ void flush(const Item &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
+                      int &n_tasks, int &n_blk, int &blk_cur) {
+    const int lane = threadIdx.x & 31;
+    while (n_tasks > 0 || n_blk > 0) {
+        for (int t0 = 0; t0 < n_tasks; t0 += 32) {
+            const int i = t0 + lane;
+            if (i < n_tasks) {
+                const int s_h = wq.task_s[i], q = wq.task_q[i];
+                const int ci = __ldg(it.gctx + q);
+                const HbgContext C = a.contexts[ci];
+                const HbgQueryDesc Q = a.queries[C.query];
+                const int ql = q - Q.start;
+                const Ext e = extend_two_hit(sh.matrix, it.s, it.S, it.gseq + Q.start, Q.len,
+                                             wq.task_left[i], s_h, ql, C.x_dropoff);
+                atomicAdd(&sh.q_ext[C.query - it.first_query], 1u);
+                if (e.score >= C.cutoff) {
+                    atomicAdd(&sh.q_kept[C.query - it.first_query], 1u);
+                    const unsigned long long o = atomicAdd(a.hsp_count, 1ull);
+                    if ((long long)o < a.hsp_cap) {
+                        hbg_hsp out;
+                        out.query = C.query;
+                        out.subject = it.j;
+                        out.q_start = e.q_start;
+                        out.s_start = e.s_start;
+                        out.q_off = ql;
+                        out.s_off = s_h;
+                        out.len = e.len;
+                        out.score = e.score;
+                        out.context = C.local;
+                        a.hsps[o] = out;
+                    }
+                }
+                const int d = (q - s_h) & it.mask;
+                it.diag[d] = e.right ? (kFlag | (uint32_t)(e.s_last_off - 2 + it.dofs))
+                                     : (uint32_t)(s_h + it.dofs);
+            }
+        }
+        __syncwarp();
+        n_tasks = 0;
+        const int nb = n_blk;
+        const int src = blk_cur;
+        n_blk = 0;
+        blk_cur ^= 1;
+        for (int b0 = 0; b0 < nb; b0 += 32) {
+            const int i = b0 + lane;
+            const bool act = i < nb;
+            int s_h = 0, q = 0, d = 0;
+            if (act) {
+                s_h = wq.blk_s[src][i];
+                q = wq.blk_q[src][i];
+                d = (q - s_h) & it.mask;
+            }
+            apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
+        }
+    }
+}
 
 }  // namespace
 
@@ -150,7 +295,9 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
-    uint32_t *diag_s = reinterpret_cast<uint32_t *>(smem_raw + sizeof(Smem)) + warp * kSmemDiag;
+    WarpQueue &wq = reinterpret_cast<WarpQueue *>(smem_raw + sizeof(Smem))[warp];
+    uint32_t *diag_s =
+        reinterpret_cast<uint32_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * kSmemDiag;
     uint32_t *diag_g =
         a.gdiag ? a.gdiag + ((size_t)blockIdx.x * nwarps + warp) * (size_t)a.gdiag_len : nullptr;
 
@@ -161,6 +308,7 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
     int32_t dofs_s = a.window, dofs_g = a.window;
     int cur_group = -1;
     const int window = a.window;
+    int n_tasks = 0, n_blk = 0, blk_cur = 0;
 
     for (;;) {
         __syncthreads();
@@ -189,11 +337,14 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
         const HbgGroup G = a.groups[g];
         const uint32_t *cs = a.cells + (size_t)g * HBG_CELL_STRIDE;
         const uint16_t *ents = a.entries + G.entry_base;
-        const uint8_t *gseq = a.letters + G.seq_base;
-        const int32_t *gctx = a.ctx_of + G.seq_base;
-        const int32_t mask = G.diag_len - 1;
-        uint32_t *diag = G.placement ? diag_g : diag_s;
-        int32_t dofs = G.placement ? dofs_g : dofs_s;
+        Item it;
+        it.diag = G.placement ? diag_g : diag_s;
+        it.mask = G.diag_len - 1;
+        it.dofs = G.placement ? dofs_g : dofs_s;
+        it.window = window;
+        it.gseq = a.letters + G.seq_base;
+        it.gctx = a.ctx_of + G.seq_base;
+        it.first_query = G.first_query;
         const int diag_alloc = G.placement ? a.gdiag_len : kSmemDiag;
 
         for (;;) {
@@ -204,16 +355,31 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
             const long long idx = (long long)blk * a.tile_subjects + k;
             if (k >= a.tile_subjects || idx >= a.n_subj)
                 break;
-            const int j = a.order[idx];
-            const uint8_t *s = a.db + a.db_off[j];
-            const int S = a.db_len[j];
+            it.j = a.order[idx];
+            it.s = a.db + a.db_off[it.j];
+            it.S = a.db_len[it.j];
             unsigned long long item_hits = 0;
 
-            for (int s0 = 0; s0 <= S - 3; s0 += 32) {
+            for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
+                // letters s0+lane, +1, +2: one coalesced load, two shuffles; the
+                // database has sentinels and tail padding, so reading past the
+                // subject end stays inside the allocation
                 const int sp = s0 + lane;
+                const uint32_t b0 = it.s[sp];
+                const uint32_t x = lane < 2 ? (uint32_t)it.s[s0 + 32 + lane] : 0u;
+                uint32_t b1 = __shfl_down_sync(0xffffffffu, b0, 1);
+                uint32_t b2 = __shfl_down_sync(0xffffffffu, b0, 2);
+                const uint32_t x0 = __shfl_sync(0xffffffffu, x, 0);
+                const uint32_t x1 = __shfl_sync(0xffffffffu, x, 1);
+                if (lane == 31) {
+                    b1 = x0;
+                    b2 = x1;
+                } else if (lane == 30) {
+                    b2 = x0;
+                }
                 uint32_t c = 0, base = 0;
-                if (sp <= S - 3) {
-                    const int w = ((int)s[sp] << 10) | ((int)s[sp + 1] << 5) | (int)s[sp + 2];
+                if (sp <= it.S - 3) {
+                    const uint32_t w = (b0 << 10) | (b1 << 5) | b2;
                     if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
                         base = __ldg(cs + w);
                         c = __ldg(cs + w + 1) - base;
@@ -222,7 +388,7 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
                 uint32_t incl = c;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= o)
                         incl += t;
                 }
@@ -237,87 +403,40 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
                     int lo = 0;
 #pragma unroll
                     for (int step = 16; step > 0; step >>= 1) {
-                        uint32_t v = __shfl_sync(0xffffffffu, excl, lo + step);
+                        const uint32_t v = __shfl_sync(0xffffffffu, excl, lo + step);
                         if (v <= h)
                             lo += step;
                     }
                     const int s_h = s0 + lo;
                     const uint32_t r = __shfl_sync(0xffffffffu, rel, lo);
-                    int q = 0, d = 0, rank = 0;
-                    const unsigned am = __ballot_sync(0xffffffffu, act);
+                    int q = 0, d = 0;
                     if (act) {
                         q = __ldg(ents + (r + h));
-                        d = (q - s_h) & mask;
-                        const unsigned grp = __match_any_sync(am, d);
-                        rank = __popc(grp & lanemask_lt());
+                        d = (q - s_h) & it.mask;
                     }
-                    bool pending = act;
-                    for (int rr = 0;; ++rr) {
-                        if (pending && rank == rr) {
-                            pending = false;
-                            const uint32_t cell = diag[d];
-                            const int32_t last = (int32_t)(cell & kLast);
-                            if (cell & kFlag) {
-                                if (s_h + dofs >= last)
-                                    diag[d] = (uint32_t)(s_h + dofs);
-                            } else {
-                                const int32_t diff = s_h - (last - dofs);
-                                if (diff >= window) {
-                                    diag[d] = (uint32_t)(s_h + dofs);
-                                } else if (diff >= 3) {
-                                    const int ci = __ldg(gctx + q);
-                                    const HbgContext C = a.contexts[ci];
-                                    const HbgQueryDesc Q = a.queries[C.query];
-                                    const int ql = q - Q.start;
-                                    const Ext e = extend_two_hit(
-                                        sh.matrix, s, S, gseq + Q.start, Q.len,
-                                        (last - dofs) + 3, s_h, ql, C.x_dropoff);
-                                    atomicAdd(&sh.q_ext[C.query - G.first_query], 1u);
-                                    if (e.score >= C.cutoff) {
-                                        atomicAdd(&sh.q_kept[C.query - G.first_query], 1u);
-                                        const unsigned long long o = atomicAdd(a.hsp_count, 1ull);
-                                        if ((long long)o < a.hsp_cap) {
-                                            hbg_hsp out;
-                                            out.query = C.query;
-                                            out.subject = j;
-                                            out.q_start = e.q_start;
-                                            out.s_start = e.s_start;
-                                            out.q_off = ql;
-                                            out.s_off = s_h;
-                                            out.len = e.len;
-                                            out.score = e.score;
-                                            out.context = C.local;
-                                            a.hsps[o] = out;
-                                        }
-                                    }
-                                    diag[d] = e.right ? (kFlag | (uint32_t)(e.s_last_off - 2 + dofs))
-                                                      : (uint32_t)(s_h + dofs);
-                                }
-                            }
-                        }
-                        __syncwarp();
-                        if (!__any_sync(0xffffffffu, pending))
-                            break;
-                    }
+                    apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
+                    if (n_tasks >= 32 || n_blk >= 32)
+                        flush(it, a, sh, wq, n_tasks, n_blk, blk_cur);
                 }
             }
+            flush(it, a, sh, wq, n_tasks, n_blk, blk_cur);
             if (lane == 0)
                 atomicAdd(&sh.hits, item_hits);
             // advance the diagonal offset past this subject (NCBI Blast_ExtendWordExit)
-            if (dofs >= kWrap) {
+            if (it.dofs >= kWrap) {
                 __syncwarp();
                 for (int i = lane; i < diag_alloc; i += 32)
-                    diag[i] = 0;
+                    it.diag[i] = 0;
                 __syncwarp();
-                dofs = window;
+                it.dofs = window;
             } else {
-                dofs += S + window;
+                it.dofs += it.S + window;
             }
         }
         if (G.placement)
-            dofs_g = dofs;
+            dofs_g = it.dofs;
         else
-            dofs_s = dofs;
+            dofs_s = it.dofs;
         __syncthreads();
         for (int i = threadIdx.x; i < G.n_queries && i < kMaxQ; i += blockDim.x) {
             if (sh.q_ext[i])
@@ -331,7 +450,7 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
 }
 
 size_t wordfinder_smem_bytes(int threads) {
-    return sizeof(Smem) + (size_t)(threads / 32) * kSmemDiag * sizeof(uint32_t);
+    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + kSmemDiag * sizeof(uint32_t));
 }
 
 cudaError_t wordfinder_configure() {
