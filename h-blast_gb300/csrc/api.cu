@@ -119,6 +119,7 @@ struct hbg_result {
     unsigned int *d_tile = nullptr;
     uint32_t *d_gdiag = nullptr;
     int64_t gdiag_entries = 0;
+    int32_t gdiag_len = 0;   // entries per (CTA, warp) slice of the global diagonal tables
     uint64_t *d_keys = nullptr;
     uint32_t *d_vals = nullptr;
     uint32_t *d_hist = nullptr;
@@ -176,6 +177,16 @@ int upload_batch(hbg_batch *b, int device) {
     return HBG_OK;
 }
 
+// Length of the per-warp global diagonal table: groups too long for shared
+// memory, and subjects whose offsets do not fit the 16-bit shared cells
+// (window + length > 32767), use it.
+int32_t global_diag_len(const hbg::HostBatch &h, const hbg_db *db) {
+    int32_t len = h.max_diag_len;
+    if (db->max_len + h.window > 0x7fff)
+        len = std::max<int32_t>(len, hbg::kSmemDiagLen);
+    return len;
+}
+
 void free_result_device(hbg_result *r) {
     dfree(r->d_raw);
     dfree(r->d_sorted);
@@ -208,8 +219,9 @@ int prepare_result(hbg_result *r, int64_t cap) {
         for (auto &e : r->ev)
             CU(cudaEventCreate(&e));
     }
-    if (h.max_diag_len > 0) {
-        const int64_t need = (int64_t)r->blocks * (r->threads / 32) * h.max_diag_len;
+    r->gdiag_len = global_diag_len(h, r->db);
+    if (r->gdiag_len > 0) {
+        const int64_t need = (int64_t)r->blocks * (r->threads / 32) * r->gdiag_len;
         if (need > r->gdiag_entries) {
             dfree(r->d_gdiag);
             CU(dalloc(&r->d_gdiag, (size_t)need));
@@ -271,7 +283,7 @@ int launch_search(hbg_result *r) {
     a.q_kept = r->d_counters + 1 + nq;
     a.g_hits = r->d_counters + 1 + 3 * nq;
     a.gdiag = r->d_gdiag;
-    a.gdiag_len = h.max_diag_len;
+    a.gdiag_len = r->gdiag_len;
 
     CU(cudaEventRecord(r->ev[0], st));
     if (db->n > 0) {
@@ -679,10 +691,10 @@ int hbg_mem_required(const hbg_db *db, const hbg_batch *b, int64_t cap, int64_t 
                                     h.entries.size() * 2 + h.pv.size() * 4 + h.query_cells.size() * 2);
     int64_t per_hsp = 2 * (int64_t)sizeof(hbg_hsp) + 2 * 8 + 2 * 4;
     int64_t gdiag = 0;
-    if (h.max_diag_len > 0) {
+    if (global_diag_len(h, db) > 0) {
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
-        gdiag = (int64_t)sms * 8 * 8 * h.max_diag_len * 4;
+        gdiag = (int64_t)sms * 8 * 8 * global_diag_len(h, db) * 4;
     }
     *bytes = batch_bytes + cap * per_hsp + gdiag + 1024 * 1024;
     return HBG_OK;

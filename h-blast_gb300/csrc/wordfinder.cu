@@ -32,11 +32,8 @@ namespace hbg {
 
 namespace {
 
-constexpr int kSmemDiag = 2048;   // must equal kSmemDiagLen in batch_builder.h
+constexpr int kSmemDiag = 4096;   // entries per warp; must equal kSmemDiagLen in batch_builder.h
 constexpr int kMaxQ = 64;         // kMaxQueriesPerGroup
-constexpr uint32_t kFlag = 0x80000000u;
-constexpr uint32_t kLast = 0x7fffffffu;
-constexpr int32_t kWrap = 1 << 29;  // offset + subject length stays below 2^31 - 1
 
 __constant__ int8_t c_blosum[28 * 32] = {
 #include "blosum62.inc"
@@ -142,6 +139,30 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return r;
 }
 // ---------------------------------------------------------------------------
+// Diagonal cells.  NCBI's DiagStruct keeps a 31-bit last hit and a 1-bit flag
+// against an offset that grows by subject length + window per subject.  The
+// shared-memory tables use 16-bit cells (15-bit last hit): the offset is
+// reset and the table cleared whenever offset + subject length would not fit,
+// so every stored value stays exact.  Tables in global memory keep 32 bits.
+
+template <typename Cell>
+struct CellTraits;
+template <>
+struct CellTraits<uint16_t> {
+    static constexpr uint32_t kFlag = 0x8000u;
+    static constexpr uint32_t kLast = 0x7fffu;
+    static constexpr int32_t kLimit = 0x7fff;       // offset + subject length must stay <= this
+};
+template <>
+struct CellTraits<uint32_t> {
+    static constexpr uint32_t kFlag = 0x80000000u;
+    static constexpr uint32_t kLast = 0x7fffffffu;
+    static constexpr int32_t kLimit = 0x7fffffff - 1;
+};
+// 32-bit tables are cleared once the offset passes this (NCBI clears at INT4_MAX/4)
+constexpr int32_t kWrap32 = 1 << 29;
+
+// ---------------------------------------------------------------------------
 // Per-warp state.  Extensions are queued and run one lane per extension; the
 // diagonal of a queued extension holds a "pending" marker (flag bit + the
 // current offset - 1, a value no real state of this subject can take, and one
@@ -159,13 +180,14 @@ struct WarpQueue {
     int blk_q[2][kQueue];
 };
 
+template <typename Cell>
 struct Item {
     const uint8_t *s;        // subject letters
     int S;                   // subject length
     int j;                   // subject ordinal id
-    uint32_t *diag;
+    Cell *diag;
     int mask;
-    int dofs;                // NCBI diagonal offset for this subject
+    int dofs;                // diagonal offset for this subject
     int window;
     const uint8_t *gseq;
     const int32_t *gctx;
@@ -174,66 +196,74 @@ struct Item {
 
 // Apply one batch of hits (one per active lane, in CPU order by lane) to the
 // diagonal table.  Lanes sharing a diagonal go in lane order.  Warp-collective.
-__device__ __forceinline__ void apply_hits(const Item &it, bool act, int d, int s_h, int q,
+template <typename Cell>
+__device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d, int s_h, int q,
                                            WarpQueue &wq, int &n_tasks, int &n_blk, int blk_out) {
+    using T = CellTraits<Cell>;
     const unsigned am = __ballot_sync(0xffffffffu, act);
-    int rank = 0;
+    int rank = 0, maxrank = 0;
     if (act) {
         const unsigned grp = __match_any_sync(am, d);
         rank = __popc(grp & lanemask_lt());
+        maxrank = __popc(grp) - 1;
     }
-    bool pending = act;
-    const uint32_t pend = kFlag | (uint32_t)(it.dofs - 1);
-    for (int rr = 0;; ++rr) {
-        bool want_task = false, want_blk = false;
-        int left = 0;
-        if (pending && rank == rr) {
-            pending = false;
+    maxrank = __reduce_max_sync(0xffffffffu, (unsigned)maxrank);
+    const uint32_t pend = T::kFlag | (uint32_t)(it.dofs - 1);
+    bool want_task = false, want_blk = false;
+    int left = 0;
+    for (int rr = 0; rr <= maxrank; ++rr) {
+        if (act && rank == rr) {
             const uint32_t cell = it.diag[d];
             if (cell == pend) {
                 want_blk = true;
-            } else if (cell & kFlag) {
-                if (s_h + it.dofs >= (int32_t)(cell & kLast))
-                    it.diag[d] = (uint32_t)(s_h + it.dofs);
+            } else if (cell & T::kFlag) {
+                if (s_h + it.dofs >= (int32_t)(cell & T::kLast))
+                    it.diag[d] = (Cell)(s_h + it.dofs);
             } else {
                 const int32_t last = (int32_t)cell - it.dofs;   // subject offset of the last hit
                 const int32_t diff = s_h - last;
                 if (diff >= it.window) {
-                    it.diag[d] = (uint32_t)(s_h + it.dofs);
+                    it.diag[d] = (Cell)(s_h + it.dofs);
                 } else if (diff >= 3) {
                     want_task = true;
                     left = last + 3;
-                    it.diag[d] = pend;
+                    it.diag[d] = (Cell)pend;
                 }
             }
         }
-        const unsigned tm = __ballot_sync(0xffffffffu, want_task);
-        if (want_task) {
-            const int p = n_tasks + __popc(tm & lanemask_lt());
-            wq.task_s[p] = s_h;
-            wq.task_q[p] = q;
-            wq.task_left[p] = left;
-        }
-        n_tasks += __popc(tm);
-        const unsigned bm = __ballot_sync(0xffffffffu, want_blk);
-        if (want_blk) {
-            const int p = n_blk + __popc(bm & lanemask_lt());
-            wq.blk_s[blk_out][p] = s_h;
-            wq.blk_q[blk_out][p] = q;
-        }
-        n_blk += __popc(bm);
         __syncwarp();
-        if (!__any_sync(0xffffffffu, pending))
-            break;
     }
+    // queue appends: tasks in any order; blocked hits in lane order, which
+    // keeps hits of one diagonal in CPU order
+    const unsigned tm = __ballot_sync(0xffffffffu, want_task);
+    if (want_task) {
+        const int p = n_tasks + __popc(tm & lanemask_lt());
+        wq.task_s[p] = s_h;
+        wq.task_q[p] = q;
+        wq.task_left[p] = left;
+    }
+    n_tasks += __popc(tm);
+    const unsigned bm = __ballot_sync(0xffffffffu, want_blk);
+    if (want_blk) {
+        const int p = n_blk + __popc(bm & lanemask_lt());
+        wq.blk_s[blk_out][p] = s_h;
+        wq.blk_q[blk_out][p] = q;
+    }
+    n_blk += __popc(bm);
+    __syncwarp();
 }
 
-// Run every queued extension (lane per extension), then replay the blocked
-// hits in order, until neither list has work.  Warp-collective.
-__device__ void flush(const Item &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
-                      int &n_tasks, int &n_blk, int &blk_cur) {
+// One round: run every queued extension (lane per extension), then replay the
+// blocked hits once, in order.  Replayed hits may queue new extensions and be
+// blocked again behind them; that is safe mid-subject because every later hit
+// on a pending diagonal is blocked after them.  With drain, repeat until both
+// lists are empty (needed before the subject ends).  Warp-collective.
+template <typename Cell>
+__device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
+                      int &n_tasks, int &n_blk, int &blk_cur, bool drain) {
+    using T = CellTraits<Cell>;
     const int lane = threadIdx.x & 31;
-    while (n_tasks > 0 || n_blk > 0) {
+    do {
         for (int t0 = 0; t0 < n_tasks; t0 += 32) {
             const int i = t0 + lane;
             if (i < n_tasks) {
@@ -263,8 +293,8 @@ __device__ void flush(const Item &it, const WordFinderArgs &a, Smem &sh, WarpQue
                     }
                 }
                 const int d = (q - s_h) & it.mask;
-                it.diag[d] = e.right ? (kFlag | (uint32_t)(e.s_last_off - 2 + it.dofs))
-                                     : (uint32_t)(s_h + it.dofs);
+                it.diag[d] = e.right ? (Cell)(T::kFlag | (uint32_t)(e.s_last_off - 2 + it.dofs))
+                                     : (Cell)(s_h + it.dofs);
             }
         }
         __syncwarp();
@@ -284,7 +314,97 @@ __device__ void flush(const Item &it, const WordFinderArgs &a, Smem &sh, WarpQue
             }
             apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
         }
+    } while (drain && (n_tasks > 0 || n_blk > 0));
+}
+
+// One (group, subject) item: scan, two-hit, queued extensions.  Warp-collective.
+template <typename Cell>
+__device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
+                                           WarpQueue &wq, const uint32_t *cs, const uint16_t *ents,
+                                           int diag_alloc) {
+    using T = CellTraits<Cell>;
+    const int lane = threadIdx.x & 31;
+    // keep every stored value exact: restart the offset (and clear) when
+    // offset + subject length would not fit the cell
+    if (sizeof(Cell) == 2 ? (it.dofs + it.S > T::kLimit) : (it.dofs >= kWrap32)) {
+        __syncwarp();
+        if (sizeof(Cell) == 2 && (diag_alloc & 7) == 0) {
+            uint4 *p = reinterpret_cast<uint4 *>(it.diag);
+            for (int i = lane; i < diag_alloc / 8; i += 32)
+                p[i] = make_uint4(0, 0, 0, 0);
+        } else {
+            for (int i = lane; i < diag_alloc; i += 32)
+                it.diag[i] = 0;
+        }
+        __syncwarp();
+        it.dofs = it.window;
     }
+    int n_tasks = 0, n_blk = 0, blk_cur = 0;
+    unsigned long long item_hits = 0;
+    for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
+        // letters s0+lane, +1, +2: one coalesced load, two shuffles; the
+        // database has sentinels and tail padding, so reading past the
+        // subject end stays inside the allocation
+        const int sp = s0 + lane;
+        const uint32_t b0 = it.s[sp];
+        const uint32_t x = lane < 2 ? (uint32_t)it.s[s0 + 32 + lane] : 0u;
+        uint32_t b1 = __shfl_down_sync(0xffffffffu, b0, 1);
+        uint32_t b2 = __shfl_down_sync(0xffffffffu, b0, 2);
+        const uint32_t x0 = __shfl_sync(0xffffffffu, x, 0);
+        const uint32_t x1 = __shfl_sync(0xffffffffu, x, 1);
+        if (lane == 31) {
+            b1 = x0;
+            b2 = x1;
+        } else if (lane == 30) {
+            b2 = x0;
+        }
+        uint32_t c = 0, base = 0;
+        if (sp <= it.S - 3) {
+            const uint32_t w = (b0 << 10) | (b1 << 5) | b2;
+            if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
+                base = __ldg(cs + w);
+                c = __ldg(cs + w + 1) - base;
+            }
+        }
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        const uint32_t T_ = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t excl = incl - c;
+        const uint32_t rel = base - excl;  // entry index of hit h = rel(owner) + h
+        item_hits += T_;
+
+        for (uint32_t hb = 0; hb < T_; hb += 32) {
+            const uint32_t h = hb + lane;
+            const bool act = h < T_;
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const uint32_t v = __shfl_sync(0xffffffffu, excl, lo + step);
+                if (v <= h)
+                    lo += step;
+            }
+            const int s_h = s0 + lo;
+            const uint32_t r = __shfl_sync(0xffffffffu, rel, lo);
+            int q = 0, d = 0;
+            if (act) {
+                q = __ldg(ents + (r + h));
+                d = (q - s_h) & it.mask;
+            }
+            apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
+            // queues hold 64: keep room for one more batch of 32
+            while (n_tasks >= 32 || n_blk >= 32)
+                flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
+        }
+    }
+    flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
+    // advance the diagonal offset past this subject (NCBI Blast_ExtendWordExit)
+    it.dofs += it.S + it.window;
+    return item_hits;
 }
 
 }  // namespace
@@ -296,8 +416,8 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     WarpQueue &wq = reinterpret_cast<WarpQueue *>(smem_raw + sizeof(Smem))[warp];
-    uint32_t *diag_s =
-        reinterpret_cast<uint32_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * kSmemDiag;
+    uint16_t *diag_s =
+        reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * kSmemDiag;
     uint32_t *diag_g =
         a.gdiag ? a.gdiag + ((size_t)blockIdx.x * nwarps + warp) * (size_t)a.gdiag_len : nullptr;
 
@@ -305,10 +425,10 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
         sh.matrix[i] = c_blosum[i];
     for (int i = lane; i < kSmemDiag; i += 32)
         diag_s[i] = 0;
-    int32_t dofs_s = a.window, dofs_g = a.window;
-    int cur_group = -1;
     const int window = a.window;
-    int n_tasks = 0, n_blk = 0, blk_cur = 0;
+    // the 16-bit shared table starts past its limit so the first item clears it
+    int32_t dofs_s = CellTraits<uint16_t>::kLimit + 1, dofs_g = window;
+    int cur_group = -1;
 
     for (;;) {
         __syncthreads();
@@ -337,15 +457,6 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
         const HbgGroup G = a.groups[g];
         const uint32_t *cs = a.cells + (size_t)g * HBG_CELL_STRIDE;
         const uint16_t *ents = a.entries + G.entry_base;
-        Item it;
-        it.diag = G.placement ? diag_g : diag_s;
-        it.mask = G.diag_len - 1;
-        it.dofs = G.placement ? dofs_g : dofs_s;
-        it.window = window;
-        it.gseq = a.letters + G.seq_base;
-        it.gctx = a.ctx_of + G.seq_base;
-        it.first_query = G.first_query;
-        const int diag_alloc = G.placement ? a.gdiag_len : kSmemDiag;
 
         for (;;) {
             int k = 0;
@@ -355,88 +466,26 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
             const long long idx = (long long)blk * a.tile_subjects + k;
             if (k >= a.tile_subjects || idx >= a.n_subj)
                 break;
-            it.j = a.order[idx];
-            it.s = a.db + a.db_off[it.j];
-            it.S = a.db_len[it.j];
-            unsigned long long item_hits = 0;
-
-            for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
-                // letters s0+lane, +1, +2: one coalesced load, two shuffles; the
-                // database has sentinels and tail padding, so reading past the
-                // subject end stays inside the allocation
-                const int sp = s0 + lane;
-                const uint32_t b0 = it.s[sp];
-                const uint32_t x = lane < 2 ? (uint32_t)it.s[s0 + 32 + lane] : 0u;
-                uint32_t b1 = __shfl_down_sync(0xffffffffu, b0, 1);
-                uint32_t b2 = __shfl_down_sync(0xffffffffu, b0, 2);
-                const uint32_t x0 = __shfl_sync(0xffffffffu, x, 0);
-                const uint32_t x1 = __shfl_sync(0xffffffffu, x, 1);
-                if (lane == 31) {
-                    b1 = x0;
-                    b2 = x1;
-                } else if (lane == 30) {
-                    b2 = x0;
-                }
-                uint32_t c = 0, base = 0;
-                if (sp <= it.S - 3) {
-                    const uint32_t w = (b0 << 10) | (b1 << 5) | b2;
-                    if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
-                        base = __ldg(cs + w);
-                        c = __ldg(cs + w + 1) - base;
-                    }
-                }
-                uint32_t incl = c;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o)
-                        incl += t;
-                }
-                const uint32_t T = __shfl_sync(0xffffffffu, incl, 31);
-                const uint32_t excl = incl - c;
-                const uint32_t rel = base - excl;  // entry index of hit h = rel(owner) + h
-                item_hits += T;
-
-                for (uint32_t hb = 0; hb < T; hb += 32) {
-                    const uint32_t h = hb + lane;
-                    const bool act = h < T;
-                    int lo = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        const uint32_t v = __shfl_sync(0xffffffffu, excl, lo + step);
-                        if (v <= h)
-                            lo += step;
-                    }
-                    const int s_h = s0 + lo;
-                    const uint32_t r = __shfl_sync(0xffffffffu, rel, lo);
-                    int q = 0, d = 0;
-                    if (act) {
-                        q = __ldg(ents + (r + h));
-                        d = (q - s_h) & it.mask;
-                    }
-                    apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
-                    if (n_tasks >= 32 || n_blk >= 32)
-                        flush(it, a, sh, wq, n_tasks, n_blk, blk_cur);
-                }
-            }
-            flush(it, a, sh, wq, n_tasks, n_blk, blk_cur);
-            if (lane == 0)
-                atomicAdd(&sh.hits, item_hits);
-            // advance the diagonal offset past this subject (NCBI Blast_ExtendWordExit)
-            if (it.dofs >= kWrap) {
-                __syncwarp();
-                for (int i = lane; i < diag_alloc; i += 32)
-                    it.diag[i] = 0;
-                __syncwarp();
-                it.dofs = window;
+            const int j = a.order[idx];
+            const int S = a.db_len[j];
+            const uint8_t *sp = a.db + a.db_off[j];
+            unsigned long long hits;
+            // shared 16-bit table when the group fits it and window + S fits 15 bits;
+            // otherwise this warp's 32-bit slice of the global scratch
+            if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
+                Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
+                                  a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
+                hits = process_item(it, a, sh, wq, cs, ents, kSmemDiag);
+                dofs_s = it.dofs;
             } else {
-                it.dofs += it.S + window;
+                Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
+                                  a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
+                hits = process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
+                dofs_g = it.dofs;
             }
+            if (lane == 0)
+                atomicAdd(&sh.hits, hits);
         }
-        if (G.placement)
-            dofs_g = it.dofs;
-        else
-            dofs_s = it.dofs;
         __syncthreads();
         for (int i = threadIdx.x; i < G.n_queries && i < kMaxQ; i += blockDim.x) {
             if (sh.q_ext[i])
@@ -450,7 +499,7 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
 }
 
 size_t wordfinder_smem_bytes(int threads) {
-    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + kSmemDiag * sizeof(uint32_t));
+    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + kSmemDiag * sizeof(uint16_t));
 }
 
 cudaError_t wordfinder_configure() {

@@ -15,7 +15,7 @@ namespace hbg {
 
 // Shared-memory diagonal tables hold at most this many entries per warp;
 // groups whose table is longer use the global-memory scratch.
-constexpr int32_t kSmemDiagLen = 2048;
+constexpr int32_t kSmemDiagLen = 4096;
 // Queries per group are bounded so per-query counters fit in shared memory.
 constexpr int32_t kMaxQueriesPerGroup = 64;
 
