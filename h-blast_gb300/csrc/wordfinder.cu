@@ -39,7 +39,7 @@ __constant__ int8_t c_blosum[28 * 32] = {
 #include "blosum62.inc"
 };
 
-struct Smem {
+struct __align__(16) Smem {   // 16-byte size: the per-warp tables after it are cleared with 16-byte stores
     uint32_t pv[HBG_PV_WORDS];
     int8_t matrix[28 * 32];
     unsigned int q_ext[kMaxQ];
@@ -179,6 +179,9 @@ struct WarpQueue {
     int blk_s[2][kQueue];
     int blk_q[2][kQueue];
 };
+// the 16-bit tables follow Smem and the queues and are cleared 16 bytes at a time
+static_assert(sizeof(Smem) % 16 == 0 && sizeof(WarpQueue) % 16 == 0 && (kSmemDiag * 2) % 16 == 0,
+              "shared-memory regions must keep 16-byte alignment");
 
 template <typename Cell>
 struct Item {
@@ -328,7 +331,7 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     // offset + subject length would not fit the cell
     if (sizeof(Cell) == 2 ? (it.dofs + it.S > T::kLimit) : (it.dofs >= kWrap32)) {
         __syncwarp();
-        if (sizeof(Cell) == 2 && (diag_alloc & 7) == 0) {
+        if (sizeof(Cell) == 2 && (diag_alloc & 7) == 0 && (reinterpret_cast<uintptr_t>(it.diag) & 15) == 0) {
             uint4 *p = reinterpret_cast<uint4 *>(it.diag);
             for (int i = lane; i < diag_alloc / 8; i += 32)
                 p[i] = make_uint4(0, 0, 0, 0);
