@@ -135,6 +135,9 @@ struct hbg_result {
     bool launched = false, synced = false, done = false;
     float wf_ms = 0.f, ord_ms = 0.f;
     int32_t launches = 0;   // kernels per search
+    int64_t launch_count = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    long long graph_key[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -183,11 +186,14 @@ int upload_batch(hbg_batch *b, int device) {
 int32_t global_diag_len(const hbg::HostBatch &h, const hbg_db *db) {
     int32_t len = h.max_diag_len;
     if (db->max_len + h.window > 0x7fff)
-        len = std::max<int32_t>(len, hbg::kSmemDiagLen);
+        len = std::max<int32_t>(len, h.smem_diag_len);
     return len;
 }
 
 void free_result_device(hbg_result *r) {
+    if (r->graph_exec)
+        cudaGraphExecDestroy(r->graph_exec);
+    r->graph_exec = nullptr;
     dfree(r->d_raw);
     dfree(r->d_sorted);
     dfree(r->d_counters);
@@ -244,7 +250,10 @@ int prepare_result(hbg_result *r, int64_t cap) {
     return HBG_OK;
 }
 
-int launch_search(hbg_result *r) {
+// Enqueue one search on r->stream: counter resets, the word finder, the
+// ordering pass, the lookup-hit counters and the copy of the counters to
+// pinned host memory.  No host synchronisation, so it can be captured.
+int enqueue_search(hbg_result *r) {
     hbg_db *db = r->db;
     const hbg::HostBatch &h = r->batch->host;
     const size_t nq = h.queries.size(), ng = h.groups.size();
@@ -284,12 +293,11 @@ int launch_search(hbg_result *r) {
     a.g_hits = r->d_counters + 1 + 3 * nq;
     a.gdiag = r->d_gdiag;
     a.gdiag_len = r->gdiag_len;
+    a.smem_diag = h.smem_diag_len;
 
     CU(cudaEventRecord(r->ev[0], st));
-    if (db->n > 0) {
-        CU(hbg::wordfinder_configure());
+    if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
         CU(hbg::launch_wordfinder(a, r->blocks, r->threads, st));
-    }
     CU(cudaEventRecord(r->ev[1], st));
 
     hbg::OrderArgs o;
@@ -319,6 +327,52 @@ int launch_search(hbg_result *r) {
     CU(cudaEventRecord(r->ev[2], st));
     CU(cudaMemcpyAsync(r->h_counters, r->d_counters, r->n_counters * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, st));
+    return HBG_OK;
+}
+
+void drop_graph(hbg_result *r) {
+    if (r->graph_exec)
+        cudaGraphExecDestroy(r->graph_exec);
+    r->graph_exec = nullptr;
+}
+
+// Launch a search.  A result that is launched again on the same non-default
+// stream with the same buffers replays a CUDA graph of the whole sequence
+// (captured on its second launch) instead of ~30 separate launches.
+int launch_search(hbg_result *r) {
+    CU(hbg::wordfinder_configure());
+    const bool graphable = r->stream != nullptr && r->launch_count > 0;
+    const long long key[5] = {(long long)r->cap, r->blocks, r->threads, (long long)r->gdiag_entries,
+                              (long long)(uintptr_t)r->stream};
+    if (!graphable) {
+        int rc = enqueue_search(r);
+        if (rc != HBG_OK)
+            return rc;
+    } else {
+        if (!r->graph_exec || memcmp(key, r->graph_key, sizeof(key)) != 0) {
+            drop_graph(r);
+            cudaGraph_t graph = nullptr;
+            CU(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_search(r);
+            cudaError_t e = cudaStreamEndCapture(r->stream, &graph);
+            if (rc != HBG_OK) {
+                if (graph)
+                    cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess)
+                return fail(HBG_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&r->graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                r->graph_exec = nullptr;
+                return fail(HBG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+            }
+            memcpy(r->graph_key, key, sizeof(key));
+        }
+        CU(cudaGraphLaunch(r->graph_exec, r->stream));
+    }
+    r->launch_count++;
     r->launched = true;
     r->synced = false;
     r->done = false;
@@ -641,6 +695,17 @@ int hbg_batch_lookup_table(const hbg_batch *b, int32_t g, uint32_t *cells, uint1
     return HBG_OK;
 }
 
+int hbg_batch_set_mode(hbg_batch *b, int32_t g, int32_t mode) {
+    if (!b || (mode != 0 && mode != 1) || g >= (int32_t)b->host.groups.size())
+        return fail(HBG_ERR_INVALID, "hbg_batch_set_mode: bad argument");
+    if (b->device >= 0)
+        return fail(HBG_ERR_STATE, "batch already uploaded: set modes before the first search");
+    for (int32_t i = 0; i < (int32_t)b->host.groups.size(); ++i)
+        if (g < 0 || i == g)
+            b->host.groups[i].mode = mode;
+    return HBG_OK;
+}
+
 int hbg_batch_destroy(hbg_batch *b) {
     if (!b)
         return fail(HBG_ERR_INVALID, "null batch");
@@ -730,18 +795,32 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
     }
     r->opt = o;
     r->stream = (cudaStream_t)stream;
-    r->threads = o.num_threadsx;
+    // a CTA's per-warp shared tables must fit the shared-memory carve-out:
+    // halve the CTA until they do (large groups get fewer warps per CTA)
+    {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, db->device);
+        int t = o.num_threadsx;
+        while (t > 32 && hbg::wordfinder_smem_bytes(t, batch->host.smem_diag_len) > (size_t)optin)
+            t = ((t / 2) + 31) / 32 * 32;
+        if (hbg::wordfinder_smem_bytes(t, batch->host.smem_diag_len) > (size_t)optin) {
+            if (!*out)
+                delete r;
+            return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
+        }
+        r->threads = t;
+    }
+    if (hbg::wordfinder_configure() != cudaSuccess) {
+        if (!*out)
+            delete r;
+        return fail(HBG_ERR_CUDA, "cannot configure the word-finder kernel (wrong GPU?)");
+    }
     if (o.num_blocksx > 0) {
         r->blocks = o.num_blocksx;
     } else {
         int sms = 1, per = 1;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
-        if (hbg::wordfinder_configure() != cudaSuccess) {
-            if (!*out)
-                delete r;
-            return fail(HBG_ERR_CUDA, "cannot configure the word-finder kernel (wrong GPU?)");
-        }
-        if (hbg::wordfinder_occupancy(r->threads, &per) != cudaSuccess || per < 1)
+        if (hbg::wordfinder_occupancy(r->threads, batch->host.smem_diag_len, &per) != cudaSuccess || per < 1)
             per = 1;
         r->blocks = sms * per;
     }

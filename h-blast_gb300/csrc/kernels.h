@@ -44,12 +44,14 @@ struct WordFinderArgs {
     // gdiag_len entries per (block, warp), zeroed before launch
     uint32_t *gdiag;
     int32_t gdiag_len;
+    // entries per warp of the 16-bit shared-memory tables (a multiple of 8)
+    int32_t smem_diag;
 };
 
 // Shared memory the word-finder kernel needs for a CTA of `threads` threads.
-size_t wordfinder_smem_bytes(int threads);
+size_t wordfinder_smem_bytes(int threads, int smem_diag);
 cudaError_t wordfinder_configure();
-cudaError_t wordfinder_occupancy(int threads, int *blocks_per_sm);
+cudaError_t wordfinder_occupancy(int threads, int smem_diag, int *blocks_per_sm);
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int blocks, int threads,
                               cudaStream_t stream);
 

@@ -7,18 +7,19 @@
 //
 // Per item the warp scans the subject 32 offsets at a time: lane l computes
 // the 15-bit word index of offset s0+l, tests the group's presence vector in
-// shared memory and reads the cell bounds; a warp scan turns the cell sizes
-// into a compacted (offset, query offset) hit list in the order the CPU word
-// finder visits hits (subject offset, then ascending query offset), which the
-// warp then processes 32 hits at a time.  Hits of one batch that fall on the
-// same diagonal are found with match.any and applied in order.
+// shared memory and reads the cell bounds.  Hits are then applied in the
+// order the CPU word finder visits them (subject offset, then ascending query
+// offset) in one of two modes chosen per group: chunk mode (sparse groups) --
+// a warp scan compacts the chunk's hits and 32 are applied at a time, hits of
+// one batch on the same diagonal ordered with match.any; offset mode (dense
+// groups) -- one offset at a time, lane i taking entry i of its cell.
 //
-// Diagonal state follows NCBI's DiagStruct (31-bit last hit + 1-bit flag) and
-// its offset trick: the offset grows by subject length + window per item so
-// stale entries read as "no recent hit", and the table is cleared when the
-// offset passes 2^30 (Blast_ExtendWordExit; H-BLAST h_blast_kernel.cu:1023).
-// Each warp owns a table of kSmemDiagLen entries in shared memory, or a slice
-// of the global scratch for groups whose table is longer.
+// Diagonal state follows NCBI's DiagStruct (last hit + flag) and its offset
+// trick: the offset grows by subject length + window per item so stale
+// entries read as "no recent hit", and the table is cleared when the offset
+// no longer fits (Blast_ExtendWordExit; H-BLAST h_blast_kernel.cu:1023).  Each
+// warp owns a 16-bit table in shared memory, or a 32-bit slice of the global
+// scratch for groups (or subjects) too long for it.
 //
 // The per-hit rule is the two-hit state machine of NCBI aa_ungapped.c, which
 // H-BLAST restates at h_blast_kernel.cu:672-871; the extension is
@@ -32,7 +33,6 @@ namespace hbg {
 
 namespace {
 
-constexpr int kSmemDiag = 4096;   // entries per warp; must equal kSmemDiagLen in batch_builder.h
 constexpr int kMaxQ = 64;         // kMaxQueriesPerGroup
 
 __constant__ int8_t c_blosum[28 * 32] = {
@@ -180,8 +180,8 @@ struct WarpQueue {
     int blk_q[2][kQueue];
 };
 // the 16-bit tables follow Smem and the queues and are cleared 16 bytes at a time
-static_assert(sizeof(Smem) % 16 == 0 && sizeof(WarpQueue) % 16 == 0 && (kSmemDiag * 2) % 16 == 0,
-              "shared-memory regions must keep 16-byte alignment");
+static_assert(sizeof(Smem) % 16 == 0 && sizeof(WarpQueue) % 16 == 0,
+              "shared-memory regions must keep 16-byte alignment (table lengths are multiples of 8)");
 
 template <typename Cell>
 struct Item {
@@ -320,15 +320,12 @@ __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, W
     } while (drain && (n_tasks > 0 || n_blk > 0));
 }
 
-// One (group, subject) item: scan, two-hit, queued extensions.  Warp-collective.
+// Keep every stored value exact: restart the offset (and clear the table)
+// when offset + subject length would not fit the cell.  Warp-collective.
 template <typename Cell>
-__device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
-                                           WarpQueue &wq, const uint32_t *cs, const uint16_t *ents,
-                                           int diag_alloc) {
+__device__ __forceinline__ void restart_offset(Item<Cell> &it, int diag_alloc) {
     using T = CellTraits<Cell>;
     const int lane = threadIdx.x & 31;
-    // keep every stored value exact: restart the offset (and clear) when
-    // offset + subject length would not fit the cell
     if (sizeof(Cell) == 2 ? (it.dofs + it.S > T::kLimit) : (it.dofs >= kWrap32)) {
         __syncwarp();
         if (sizeof(Cell) == 2 && (diag_alloc & 7) == 0 && (reinterpret_cast<uintptr_t>(it.diag) & 15) == 0) {
@@ -342,33 +339,55 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
         __syncwarp();
         it.dofs = it.window;
     }
+}
+
+// Word index of offset s0+lane, presence test and cell bounds:
+// *c = hits of that offset, *base = first entry.  Warp-collective.
+template <typename Cell>
+__device__ __forceinline__ void scan_words(const Item<Cell> &it, const Smem &sh, const uint32_t *cs,
+                                           int s0, uint32_t *c, uint32_t *base) {
+    const int lane = threadIdx.x & 31;
+    // letters s0+lane, +1, +2: one coalesced load, two shuffles; the
+    // database has sentinels and tail padding, so reading past the
+    // subject end stays inside the allocation
+    const int sp = s0 + lane;
+    const uint32_t b0 = it.s[sp];
+    const uint32_t x = lane < 2 ? (uint32_t)it.s[s0 + 32 + lane] : 0u;
+    uint32_t b1 = __shfl_down_sync(0xffffffffu, b0, 1);
+    uint32_t b2 = __shfl_down_sync(0xffffffffu, b0, 2);
+    const uint32_t x0 = __shfl_sync(0xffffffffu, x, 0);
+    const uint32_t x1 = __shfl_sync(0xffffffffu, x, 1);
+    if (lane == 31) {
+        b1 = x0;
+        b2 = x1;
+    } else if (lane == 30) {
+        b2 = x0;
+    }
+    *c = 0;
+    *base = 0;
+    if (sp <= it.S - 3) {
+        const uint32_t w = (b0 << 10) | (b1 << 5) | b2;
+        if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
+            *base = __ldg(cs + w);
+            *c = __ldg(cs + w + 1) - *base;
+        }
+    }
+}
+
+// Chunk mode, for sparse groups: one (group, subject) item scanned 32
+// offsets at a time, the hits of the chunk compacted in CPU order and applied
+// 32 at a time.  Warp-collective.
+template <typename Cell>
+__device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
+                                           WarpQueue &wq, const uint32_t *cs, const uint16_t *ents,
+                                           int diag_alloc) {
+    const int lane = threadIdx.x & 31;
+    restart_offset(it, diag_alloc);
     int n_tasks = 0, n_blk = 0, blk_cur = 0;
     unsigned long long item_hits = 0;
     for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
-        // letters s0+lane, +1, +2: one coalesced load, two shuffles; the
-        // database has sentinels and tail padding, so reading past the
-        // subject end stays inside the allocation
-        const int sp = s0 + lane;
-        const uint32_t b0 = it.s[sp];
-        const uint32_t x = lane < 2 ? (uint32_t)it.s[s0 + 32 + lane] : 0u;
-        uint32_t b1 = __shfl_down_sync(0xffffffffu, b0, 1);
-        uint32_t b2 = __shfl_down_sync(0xffffffffu, b0, 2);
-        const uint32_t x0 = __shfl_sync(0xffffffffu, x, 0);
-        const uint32_t x1 = __shfl_sync(0xffffffffu, x, 1);
-        if (lane == 31) {
-            b1 = x0;
-            b2 = x1;
-        } else if (lane == 30) {
-            b2 = x0;
-        }
-        uint32_t c = 0, base = 0;
-        if (sp <= it.S - 3) {
-            const uint32_t w = (b0 << 10) | (b1 << 5) | b2;
-            if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
-                base = __ldg(cs + w);
-                c = __ldg(cs + w + 1) - base;
-            }
-        }
+        uint32_t c, base;
+        scan_words(it, sh, cs, s0, &c, &base);
         uint32_t incl = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -410,6 +429,112 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     return item_hits;
 }
 
+
+// ---------------------------------------------------------------------------
+// Per-offset mode, for groups dense enough that one subject offset has many
+// hits: the warp visits the offsets in order and lane i takes entry i of the
+// offset's cell (contiguous, so the load is coalesced).  Hits of one offset
+// lie on distinct diagonals, so they need no ordering among themselves; the
+// next offset's first 32 entries are loaded while this one is applied.
+
+template <typename Cell>
+__device__ __forceinline__ void apply_offset(const Item<Cell> &it, bool act, int s_h, int q,
+                                             WarpQueue &wq, int &n_tasks, int &n_blk, int blk_out) {
+    using T = CellTraits<Cell>;
+    const uint32_t pend = T::kFlag | (uint32_t)(it.dofs - 1);
+    bool want_task = false, want_blk = false;
+    int left = 0;
+    if (act) {
+        const int d = (q - s_h) & it.mask;
+        const uint32_t cell = it.diag[d];
+        if (cell == pend) {
+            want_blk = true;
+        } else if (cell & T::kFlag) {
+            if (s_h + it.dofs >= (int32_t)(cell & T::kLast))
+                it.diag[d] = (Cell)(s_h + it.dofs);
+        } else {
+            const int32_t last = (int32_t)cell - it.dofs;
+            const int32_t diff = s_h - last;
+            if (diff >= it.window) {
+                it.diag[d] = (Cell)(s_h + it.dofs);
+            } else if (diff >= 3) {
+                want_task = true;
+                left = last + 3;
+                it.diag[d] = (Cell)pend;
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, want_task || want_blk)) {
+        const unsigned tm = __ballot_sync(0xffffffffu, want_task);
+        if (want_task) {
+            const int p = n_tasks + __popc(tm & lanemask_lt());
+            wq.task_s[p] = s_h;
+            wq.task_q[p] = q;
+            wq.task_left[p] = left;
+        }
+        n_tasks += __popc(tm);
+        const unsigned bm = __ballot_sync(0xffffffffu, want_blk);
+        if (want_blk) {
+            const int p = n_blk + __popc(bm & lanemask_lt());
+            wq.blk_s[blk_out][p] = s_h;
+            wq.blk_q[blk_out][p] = q;
+        }
+        n_blk += __popc(bm);
+    }
+    __syncwarp();
+}
+
+template <typename Cell>
+__device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
+                                                   WarpQueue &wq, const uint32_t *cs,
+                                                   const uint16_t *ents, int diag_alloc) {
+    const int lane = threadIdx.x & 31;
+    restart_offset(it, diag_alloc);
+    int n_tasks = 0, n_blk = 0, blk_cur = 0;
+    unsigned long long item_hits = 0;
+    for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
+        uint32_t c, base;
+        scan_words(it, sh, cs, s0, &c, &base);
+        item_hits += __reduce_add_sync(0xffffffffu, c);
+        unsigned m = __ballot_sync(0xffffffffu, c != 0);
+        uint32_t nb = 0, nc = 0;
+        int q_next = 0;
+        if (m) {
+            const int p = __ffs(m) - 1;
+            nb = __shfl_sync(0xffffffffu, base, p);
+            nc = __shfl_sync(0xffffffffu, c, p);
+            if ((uint32_t)lane < nc)
+                q_next = __ldg(ents + nb + lane);
+        }
+        while (m) {
+            const int p = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t cb = nb, cc = nc;
+            const int q_cur = q_next;
+            if (m) {
+                const int pn = __ffs(m) - 1;
+                nb = __shfl_sync(0xffffffffu, base, pn);
+                nc = __shfl_sync(0xffffffffu, c, pn);
+                q_next = (uint32_t)lane < nc ? __ldg(ents + nb + lane) : 0;
+            }
+            const int s_h = s0 + p;
+            apply_offset(it, (uint32_t)lane < cc, s_h, q_cur, wq, n_tasks, n_blk, blk_cur);
+            while (n_tasks >= 32 || n_blk >= 32)
+                flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
+            for (uint32_t e0 = 32; e0 < cc; e0 += 32) {
+                const bool act = e0 + lane < cc;
+                const int q = act ? __ldg(ents + cb + e0 + lane) : 0;
+                apply_offset(it, act, s_h, q, wq, n_tasks, n_blk, blk_cur);
+                while (n_tasks >= 32 || n_blk >= 32)
+                    flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
+            }
+        }
+    }
+    flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
+    it.dofs += it.S + it.window;
+    return item_hits;
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
@@ -420,13 +545,13 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
     const int nwarps = blockDim.x >> 5;
     WarpQueue &wq = reinterpret_cast<WarpQueue *>(smem_raw + sizeof(Smem))[warp];
     uint16_t *diag_s =
-        reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * kSmemDiag;
+        reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * a.smem_diag;
     uint32_t *diag_g =
         a.gdiag ? a.gdiag + ((size_t)blockIdx.x * nwarps + warp) * (size_t)a.gdiag_len : nullptr;
 
     for (int i = threadIdx.x; i < 28 * 32; i += blockDim.x)
         sh.matrix[i] = c_blosum[i];
-    for (int i = lane; i < kSmemDiag; i += 32)
+    for (int i = lane; i < a.smem_diag; i += 32)
         diag_s[i] = 0;
     const int window = a.window;
     // the 16-bit shared table starts past its limit so the first item clears it
@@ -478,12 +603,14 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
             if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = process_item(it, a, sh, wq, cs, ents, kSmemDiag);
+                hits = G.mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
+                              : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
                 dofs_s = it.dofs;
             } else {
                 Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
+                hits = G.mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
+                              : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
                 dofs_g = it.dofs;
             }
             if (lane == 0)
@@ -501,23 +628,26 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
     }
 }
 
-size_t wordfinder_smem_bytes(int threads) {
-    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + kSmemDiag * sizeof(uint16_t));
+size_t wordfinder_smem_bytes(int threads, int smem_diag) {
+    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + (size_t)smem_diag * sizeof(uint16_t));
 }
 
 cudaError_t wordfinder_configure() {
-    return cudaFuncSetAttribute(wordfinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)wordfinder_smem_bytes(256));
+    // opt in to the largest shared-memory carve-out; launches size their own
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return cudaFuncSetAttribute(wordfinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
 }
 
-cudaError_t wordfinder_occupancy(int threads, int *blocks_per_sm) {
+cudaError_t wordfinder_occupancy(int threads, int smem_diag, int *blocks_per_sm) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel, threads,
-                                                         wordfinder_smem_bytes(threads));
+                                                         wordfinder_smem_bytes(threads, smem_diag));
 }
 
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int blocks, int threads,
                               cudaStream_t stream) {
-    wordfinder_kernel<<<blocks, threads, wordfinder_smem_bytes(threads), stream>>>(a);
+    wordfinder_kernel<<<blocks, threads, wordfinder_smem_bytes(threads, a.smem_diag), stream>>>(a);
     return cudaGetLastError();
 }
 

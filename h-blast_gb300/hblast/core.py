@@ -78,6 +78,7 @@ _SIGS = {
                                          C.c_int64, C.POINTER(_P)], C.c_int),
     "hbg_batch_lookup_table": ([_P, C.c_int32, _P, _P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), _P], C.c_int),
+    "hbg_batch_set_mode": ([_P, C.c_int32, C.c_int32], C.c_int),
     "hbg_batch_destroy": ([_P], C.c_int),
     "hbg_batch_info": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
                         C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
@@ -274,6 +275,11 @@ class Batch:
         _check(lib().hbg_batch_lookup_table(self.handle, g, cells.ctypes.data, ent.ctypes.data, len(ent),
                                             C.byref(n), C.byref(fq), C.byref(nq), qs.ctypes.data))
         return cells, ent[:n.value], fq.value, qs[:nq.value]
+
+    def set_mode(self, mode: int, group: int = -1) -> "Batch":
+        """0 = chunk mode, 1 = offset mode, for one group or all (before the first search)."""
+        _check(lib().hbg_batch_set_mode(self.handle, group, mode))
+        return self
 
     def close(self):
         if self.handle:

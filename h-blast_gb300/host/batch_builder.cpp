@@ -90,13 +90,15 @@ int32_t blosum62(int32_t a, int32_t b) {
 const int8_t *blosum62_table() { return kBlosum62; }
 
 std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
-                        int32_t window, int32_t max_group_len, HostBatch *out) {
+                        int32_t window, int32_t max_group_len, HostBatch *out, double mode_hits) {
     if (window < 1 || window > 100000)
         return "window must be in 1..100000";
     if (qs.empty())
         return "empty batch";
     if (max_group_len <= 0)
-        max_group_len = kSmemDiagLen - window;
+        max_group_len = std::max<int32_t>(1, kDefaultGroupTable - window);
+    if (mode_hits < 0)
+        mode_hits = kOffsetModeHits;
     HostBatch &b = *out;
     b = HostBatch();
     b.threshold = threshold;
@@ -191,9 +193,11 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
         G.n_queries = k - G.first_query;
         G.glen = glen;
         G.diag_len = next_pow2(glen + window);
-        G.placement = G.diag_len <= kSmemDiagLen ? 0 : 1;
+        G.placement = G.diag_len <= kSmemDiagMax ? 0 : 1;
         if (G.placement)
             b.max_diag_len = std::max(b.max_diag_len, G.diag_len);
+        else
+            b.smem_diag_len = std::max(b.smem_diag_len, G.diag_len);
         seq_pos += glen;
     }
 
@@ -232,6 +236,18 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
         }
         cs[HBG_NUM_CELLS] = acc;
         G.entry_base = entry_pos;
+        // expected hits per subject offset on typical proteins: entries of
+        // words over the 20 standard letters, each such word taken as
+        // equally likely (1 / 8000)
+        {
+            static const uint8_t kStd[20] = {1, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 22};
+            uint64_t std_entries = 0;
+            for (int x = 0; x < 20; ++x)
+                for (int y = 0; y < 20; ++y)
+                    for (int z = 0; z < 20; ++z)
+                        std_entries += count[(kStd[x] << 10) | (kStd[y] << 5) | kStd[z]];
+            G.mode = (double)std_entries / 8000.0 >= mode_hits ? 1 : 0;
+        }
         b.entries.resize((size_t)(entry_pos + acc));
         // fill (ascending p inside each cell)
         std::vector<uint32_t> cursor(cs, cs + HBG_NUM_CELLS);

@@ -13,9 +13,13 @@
 
 namespace hbg {
 
-// Shared-memory diagonal tables hold at most this many entries per warp;
-// groups whose table is longer use the global-memory scratch.
-constexpr int32_t kSmemDiagLen = 4096;
+// Shared-memory diagonal tables (16-bit cells) hold at most this many
+// entries per warp; groups whose table is longer use the global scratch.
+constexpr int32_t kSmemDiagMax = 16384;
+// Default group length: the table of a full group is 8192 entries (16 KB).
+constexpr int32_t kDefaultGroupTable = 8192;
+// Groups whose expected hits per subject offset reach this use offset mode.
+constexpr double kOffsetModeHits = 6.0;
 // Queries per group are bounded so per-query counters fit in shared memory.
 constexpr int32_t kMaxQueriesPerGroup = 64;
 
@@ -33,6 +37,7 @@ struct HostBatch {
     std::vector<uint16_t> query_cells;   // queries x HBG_NUM_CELLS cell sizes
     int32_t max_query_len = 0;
     int32_t max_diag_len = 0;            // over groups with global placement
+    int32_t smem_diag_len = 64;          // per-warp shared table: max over shared-placed groups
 };
 
 // One query already in NCBI concatenated form.
@@ -43,8 +48,11 @@ struct QueryIn {
 };
 
 // Returns an empty string on success, else the reason.
+// max_group_len 0 = default; mode_hits < 0 = default offset-mode threshold,
+// 0 = offset mode for every group, a huge value = chunk mode for every group.
 std::string build_batch(const std::vector<QueryIn> &queries, int32_t threshold,
-                        int32_t window, int32_t max_group_len, HostBatch *out);
+                        int32_t window, int32_t max_group_len, HostBatch *out,
+                        double mode_hits = -1.0);
 
 // Standard-code six-frame translation (frames +1,+2,+3,-1,-2,-3, one sentinel
 // between frames).  Returns the concatenated letters; fills offsets/lengths.

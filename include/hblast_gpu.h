@@ -204,6 +204,13 @@ int hbg_batch_lookup_table(const hbg_batch *batch, int32_t g, uint32_t *cells,
                            uint16_t *entries, int64_t entries_cap, int64_t *n_entries,
                            int32_t *first_query, int32_t *n_queries, int32_t *query_start);
 
+/* Choose how group g (all groups when g < 0) applies its hits: mode 0 =
+ * chunk mode (32 offsets compacted at a time; best for sparse groups), 1 =
+ * offset mode (one subject offset at a time, lanes over its cell; best for
+ * dense groups).  The builder picks by expected hits per offset; results do
+ * not depend on the choice.  Call before the batch's first search. */
+int hbg_batch_set_mode(hbg_batch *batch, int32_t g, int32_t mode);
+
 int hbg_batch_destroy(hbg_batch *batch);
 /* Sizes of a batch; device_bytes is what its upload copies host-to-device. */
 int hbg_batch_info(const hbg_batch *batch, int32_t *n_queries, int32_t *n_groups,

@@ -3,7 +3,7 @@
 Every HSP field and the per-query counters must be identical; tolerance 0
 (integer work).  Sizes are kept where the oracle finishes in seconds; the
 full-size configurations are covered by size-independent properties in
-test_gpu_properties.py.
+test_gpu_fullsize.py.
 """
 import numpy as np
 import pytest
@@ -74,13 +74,24 @@ def test_alone_equals_in_the_mix(small_db):
         assert np.array_equal(got, alone), k
 
 
-def test_long_query_global_diagonal_table(built):
+@pytest.mark.parametrize("qlen", [9000, 20000])
+def test_long_query_tables(built, qlen):
+    # 9000: a 16384-entry shared table (4-warp CTAs); 20000: a 32768-entry
+    # table in the global scratch
     rng = np.random.default_rng(12)
-    q = synth.random_letters(rng, 6000)
-    db = synth.make_db(rng, 400, 300, 0.6, 30, 5000, 40, [q], lambda r: r.integers(100, 400), 0.5)
+    q = synth.random_letters(rng, qlen)
+    db = synth.make_db(rng, 300, 300, 0.6, 30, 5000, 40, [q], lambda r: r.integers(100, 400), 0.5)
     gdb = hblast.Database(db.residues, db.offsets)
     pqs = [hblast.ProteinQuery.blastp(q), hblast.ProteinQuery.blastp(q[:200])]
     res = hblast.search(gdb, hblast.Batch.proteins(pqs))
+    check(res, pqs, db.residues, db.offsets)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_both_hit_modes(small_db, mode):
+    qs, db, gdb = small_db
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs).set_mode(mode))
     check(res, pqs, db.residues, db.offsets)
 
 
@@ -156,3 +167,22 @@ def test_launch_shapes_do_not_change_results(small_db):
     for threads, blocks in ((32, 1), (64, 7), (256, 1000)):
         o = hblast.default_options(num_threadsx=threads, num_blocksx=blocks)
         assert np.array_equal(hblast.search(gdb, batch, options=o).hsps, base), (threads, blocks)
+
+
+def test_repeated_launches_replay_graph(small_db):
+    """A reused result on a non-default stream replays a captured CUDA graph
+    from its second launch on; every launch must give the same HSPs."""
+    import torch
+    qs, db, gdb = small_db
+    batch = hblast.Batch.proteins([hblast.ProteinQuery.blastp(q) for q in qs])
+    stream = torch.cuda.Stream()
+    s = hblast.Searcher(gdb, batch)
+    outs = []
+    for _ in range(3):
+        s.launch(stream.cuda_stream)
+        s.wait()
+        outs.append(s.result().hsps)
+    s.close()
+    ref = hblast.search(gdb, batch).hsps
+    for o in outs:
+        assert np.array_equal(o, ref)

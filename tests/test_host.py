@@ -80,12 +80,12 @@ def test_lookup_table_rare_letters(built):
 
 def test_group_packing_and_offsets(built):
     rng = np.random.default_rng(1)
-    qs = [synth.random_letters(rng, n) for n in (100, 900, 800, 50, 5000, 20)]
+    qs = [synth.random_letters(rng, n) for n in (100, 900, 800, 50, 9000, 20)]
     b = hblast.Batch.proteins([hblast.ProteinQuery.blastp(x) for x in qs])
     info = b.info()
     assert info["n_queries"] == 6
-    # 100+40+900+40+800+40+50 = 1970 <= 4056 share a group; 5000 needs its own
-    # (global-memory diagonal table); 20 cannot join it
+    # 100+40+900+40+800+40+50 = 1970 <= 8152 share a group; 9000 needs its own
+    # (a 16384-entry table); 20 cannot join it
     assert info["n_groups"] == 3
     seen = 0
     for g in range(info["n_groups"]):
