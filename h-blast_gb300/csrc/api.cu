@@ -295,10 +295,12 @@ int enqueue_search(hbg_result *r) {
     a.gdiag_len = r->gdiag_len;
     a.smem_diag = h.smem_diag_len;
 
-    CU(cudaEventRecord(r->ev[0], st));
+    // external records: inside a stream capture they become event-record
+    // nodes of the graph (usable for timing), not internal fork/join edges
+    CU(cudaEventRecordWithFlags(r->ev[0], st, cudaEventRecordExternal));
     if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
         CU(hbg::launch_wordfinder(a, r->blocks, r->threads, st));
-    CU(cudaEventRecord(r->ev[1], st));
+    CU(cudaEventRecordWithFlags(r->ev[1], st, cudaEventRecordExternal));
 
     hbg::OrderArgs o;
     memset(&o, 0, sizeof(o));
@@ -324,7 +326,7 @@ int enqueue_search(hbg_result *r) {
                       (nq > 0 ? 1 : 0);
     }
     CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
-    CU(cudaEventRecord(r->ev[2], st));
+    CU(cudaEventRecordWithFlags(r->ev[2], st, cudaEventRecordExternal));
     CU(cudaMemcpyAsync(r->h_counters, r->d_counters, r->n_counters * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, st));
     return HBG_OK;
@@ -989,3 +991,4 @@ int hbg_search_sync(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, hb
 }
 
 }  // extern "C"
+
