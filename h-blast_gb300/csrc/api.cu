@@ -295,12 +295,17 @@ int enqueue_search(hbg_result *r) {
     a.gdiag_len = r->gdiag_len;
     a.smem_diag = h.smem_diag_len;
 
-    // external records: inside a stream capture they become event-record
-    // nodes of the graph (usable for timing), not internal fork/join edges
-    CU(cudaEventRecordWithFlags(r->ev[0], st, cudaEventRecordExternal));
+    // external records while capturing: they become event-record nodes of
+    // the graph (usable for timing), not internal fork/join edges; the flag
+    // is only accepted during a capture
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(st, &cap_status));
+    const unsigned ev_flags =
+        cap_status == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    CU(cudaEventRecordWithFlags(r->ev[0], st, ev_flags));
     if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
         CU(hbg::launch_wordfinder(a, r->blocks, r->threads, st));
-    CU(cudaEventRecordWithFlags(r->ev[1], st, cudaEventRecordExternal));
+    CU(cudaEventRecordWithFlags(r->ev[1], st, ev_flags));
 
     hbg::OrderArgs o;
     memset(&o, 0, sizeof(o));
@@ -326,7 +331,7 @@ int enqueue_search(hbg_result *r) {
                       (nq > 0 ? 1 : 0);
     }
     CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
-    CU(cudaEventRecordWithFlags(r->ev[2], st, cudaEventRecordExternal));
+    CU(cudaEventRecordWithFlags(r->ev[2], st, ev_flags));
     CU(cudaMemcpyAsync(r->h_counters, r->d_counters, r->n_counters * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, st));
     return HBG_OK;
