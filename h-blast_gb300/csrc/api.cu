@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
@@ -997,3 +998,136 @@ int hbg_search_sync(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, hb
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------------
+// Search without allocation.
+//
+// For callers that may not allocate device memory at search time -- code
+// running inside a CUDA graph capture, allocator-free real-time services, or
+// hosts that hand the library a fixed memory budget up front -- this entry
+// point launches the word finder with its scratch in a file-scope device
+// array instead of cudaMalloc'd buffers.  The array is HBG_STATIC_SCRATCH_BYTES
+// on every device that loads the library and stays allocated until exit.
+
+namespace {
+
+constexpr int kStaticMaxDevices = 64;
+__device__ __align__(256) unsigned char g_static_scratch[HBG_STATIC_SCRATCH_BYTES];
+
+std::mutex g_static_mu;
+void *g_static_ptr[kStaticMaxDevices];   // device address of g_static_scratch, per device
+
+// Device address of the scratch array on `device` (current device on entry).
+// The array's name is only a host-side stand-in in host code, so the address
+// is looked up once per device with cudaGetSymbolAddress.
+int static_scratch(int device, void **out) {
+    if (device < 0 || device >= kStaticMaxDevices)
+        return fail(HBG_ERR_INVALID, "device index outside the static scratch table");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(HBG_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch): ") +
+                                          cudaGetErrorString(e));
+        g_static_ptr[device] = p;
+    }
+    *out = g_static_ptr[device];
+    return HBG_OK;
+}
+
+}  // namespace
+
+extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const hbg_gpu_options *opt,
+                                 hbg_hsp *d_hsps, int64_t hsp_cap, unsigned long long *d_counts,
+                                 void *stream) {
+    if (!db || !batch || !d_counts || hsp_cap < 0 || (hsp_cap > 0 && !d_hsps))
+        return fail(HBG_ERR_INVALID, "hbg_search_static: null argument or negative capacity");
+    if (batch->device != db->device)
+        return fail(HBG_ERR_STATE, "hbg_search_static: the batch is not resident on the database's device "
+                                   "(run hbg_search on it once during set-up)");
+    hbg_gpu_options o;
+    hbg_default_gpu_options(&o);
+    if (opt)
+        o = *opt;
+    if (!o.use_gpu)
+        return fail(HBG_ERR_NO_DEVICE, "use_gpu is 0 and this library has no CPU path");
+    if (!valid_opts(&o))
+        return fail(HBG_ERR_INVALID, "num_threadsx must be a multiple of 32 in 32..256");
+    const hbg::HostBatch &h = batch->host;
+    const int64_t nq = (int64_t)h.queries.size(), ng = (int64_t)h.groups.size();
+    // scratch layout: [tile counter | per-query extensions | per-query kept | per-group hits]
+    const int64_t need = 256 + 8 * (2 * nq + ng);
+    if (need > HBG_STATIC_SCRATCH_BYTES)
+        return fail(HBG_ERR_TOO_LONG, "hbg_search_static: the batch needs " + std::to_string(need) +
+                                          " scratch bytes, more than HBG_STATIC_SCRATCH_BYTES");
+    if (global_diag_len(h, db) > 0)
+        return fail(HBG_ERR_TOO_LONG, "hbg_search_static: groups longer than 16344 letters or subjects "
+                                      "longer than 32767 - window need global diagonal tables");
+    DeviceScope ds(db->device);
+    void *scratch = nullptr;
+    int rc = static_scratch(db->device, &scratch);
+    if (rc != HBG_OK)
+        return rc;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, db->device);
+    int threads = o.num_threadsx;
+    while (threads > 32 && hbg::wordfinder_smem_bytes(threads, h.smem_diag_len) > (size_t)optin)
+        threads = ((threads / 2) + 31) / 32 * 32;
+    if (hbg::wordfinder_smem_bytes(threads, h.smem_diag_len) > (size_t)optin)
+        return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
+    CU(hbg::wordfinder_configure());
+    int blocks = o.num_blocksx;
+    if (blocks <= 0) {
+        int sms = 1, per = 1;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
+        if (hbg::wordfinder_occupancy(threads, h.smem_diag_len, &per) != cudaSuccess || per < 1)
+            per = 1;
+        blocks = sms * per;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char *base = (unsigned char *)scratch;
+    unsigned int *tile = (unsigned int *)base;
+    unsigned long long *q_ext = (unsigned long long *)(base + 256);
+    unsigned long long *q_kept = q_ext + nq;
+    unsigned long long *g_hits = q_kept + nq;
+    // every call shares the array: clear what the kernel accumulates into
+    CU(cudaMemsetAsync(scratch, 0, (size_t)need, st));
+    CU(cudaMemsetAsync(d_counts, 0, sizeof(unsigned long long) * (size_t)(1 + 2 * nq), st));
+
+    hbg::WordFinderArgs a;
+    memset(&a, 0, sizeof(a));
+    a.db = db->d_letters;
+    a.db_off = db->d_off;
+    a.db_len = db->d_len;
+    a.order = db->d_order;
+    a.n_subj = db->n;
+    a.groups = batch->d_groups;
+    a.n_groups = (int32_t)ng;
+    a.cells = batch->d_cells;
+    a.entries = batch->d_entries;
+    a.pv = batch->d_pv;
+    a.letters = batch->d_letters;
+    a.ctx_of = batch->d_ctx_of;
+    a.contexts = batch->d_ctx;
+    a.queries = batch->d_queries;
+    a.window = h.window;
+    a.tile_subjects = 128;
+    a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
+    a.n_tiles = (int64_t)a.tiles_per_group * ng;
+    a.tile_counter = tile;
+    a.hsps = d_hsps;
+    a.hsp_count = d_counts;
+    a.hsp_cap = hsp_cap;
+    a.q_extended = q_ext;
+    a.q_kept = q_kept;
+    a.g_hits = g_hits;
+    a.gdiag = nullptr;
+    a.gdiag_len = 0;
+    a.smem_diag = h.smem_diag_len;
+    if (db->n > 0)
+        CU(hbg::launch_wordfinder(a, blocks, threads, st));
+    // per-query extension and kept counts follow the HSP count in d_counts
+    CU(cudaMemcpyAsync(d_counts + 1, q_ext, sizeof(unsigned long long) * (size_t)(2 * nq),
+                       cudaMemcpyDeviceToDevice, st));
+    return HBG_OK;
+}

@@ -94,6 +94,7 @@ _SIGS = {
     "hbg_result_free": ([_P], C.c_int),
     "hbg_search_sync": ([_P, _P, C.POINTER(GpuOptions), _P, C.c_int64, C.POINTER(C.c_int64),
                          C.POINTER(QueryStats), _P], C.c_int),
+    "hbg_search_static": ([_P, _P, C.POINTER(GpuOptions), _P, C.c_int64, _P, _P], C.c_int),
 }
 
 _lib = None

@@ -265,6 +265,44 @@ int hbg_result_stats(const hbg_result *res, int32_t q, hbg_query_stats *out);
  * h_blast.cu:1254-1278). */
 int hbg_result_free(hbg_result *res);
 
+/* ---- search without allocation -------------------------------------------- */
+
+/* Size of the device array that hbg_search_static uses for its scratch.  The
+ * array is a file-scope __device__ variable: every GPU that loads the library
+ * holds it until the process exits. */
+#define HBG_STATIC_SCRATCH_BYTES 262144
+
+/* Run the word finder without allocating anything.  No counterpart in the
+ * reference: H-BLAST allocates its buffers on every call.
+ *
+ * For callers that cannot call cudaMalloc at search time -- code running
+ * while a CUDA graph is being captured, allocator-free real-time services, or
+ * hosts that give the library a fixed memory budget at start-up.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine; its scratch (a tile
+ * counter and per-query / per-group counters, 256 + 8 x (2 x queries + groups)
+ * bytes) lives in a static device array of HBG_STATIC_SCRATCH_BYTES.
+ *
+ * Inputs: a resident database and a batch that is already resident on the
+ * same device (search it once with hbg_search during set-up).  Outputs, in
+ * caller-owned device memory: d_hsps (hsp_cap records, in no particular order;
+ * hbg_search returns the same records in reference order) and d_counts
+ * (1 + 2 x queries values: the number of HSPs found -- which may exceed
+ * hsp_cap, in which case only hsp_cap were written -- then the extensions
+ * tried per query, then the extensions kept per query).  Work is queued on
+ * stream; the call returns at once.
+ *
+ * Limits: batches whose scratch would exceed HBG_STATIC_SCRATCH_BYTES, groups
+ * longer than 16344 letters and subjects longer than 32767 - window (both need
+ * global diagonal tables) are rejected with HBG_ERR_TOO_LONG.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call uses the same array and clears it first, so calls whose work
+ * overlaps on the GPU (other streams, other threads) race: serialise them. */
+int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const hbg_gpu_options *opt,
+                      hbg_hsp *d_hsps, int64_t hsp_cap, unsigned long long *d_counts,
+                      void *stream);
+
 /* ---- one-call helper ------------------------------------------------------ */
 
 /* Host-to-host search: upload nothing that is already resident, run, wait and
