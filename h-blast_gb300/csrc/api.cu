@@ -103,6 +103,8 @@ struct hbg_batch {
     uint16_t *d_entries = nullptr;
     uint32_t *d_pv = nullptr;
     uint16_t *d_qcells = nullptr;
+    int32_t *d_group_list = nullptr;   // chunk-mode groups, then offset-mode groups
+    int32_t n_mode[2] = {0, 0};
     int64_t device_bytes = 0;
 };
 
@@ -113,7 +115,8 @@ struct hbg_result {
     cudaStream_t stream = nullptr;
     int device = 0;
     int64_t cap = 0;
-    int blocks = 0, threads = 256;
+    int blocks = 0, threads = 256;   // blocks = the larger of the two modes' grids
+    int blocks_mode[2] = {0, 0};
     // device
     hbg_hsp *d_raw = nullptr, *d_sorted = nullptr;
     unsigned long long *d_counters = nullptr;  // [0]=hsp count, then per query ext, kept, hits; per group hits
@@ -176,6 +179,20 @@ int upload_batch(hbg_batch *b, int device) {
         CU(cudaMemcpy(b->d_entries, h.entries.data(), h.entries.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_pv, h.pv.data(), h.pv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_qcells, h.query_cells.data(), h.query_cells.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    {
+        // one launch per hit mode: list the groups of each mode
+        std::vector<int32_t> list;
+        for (int mode = 0; mode < 2; ++mode) {
+            b->n_mode[mode] = 0;
+            for (int32_t g = 0; g < (int32_t)h.groups.size(); ++g)
+                if (h.groups[g].mode == mode) {
+                    list.push_back(g);
+                    b->n_mode[mode]++;
+                }
+        }
+        CU(dalloc(&b->d_group_list, list.size()));
+        CU(cudaMemcpy(b->d_group_list, list.data(), list.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
     b->device_bytes = batch_device_bytes(h);
     b->device = device;
     return HBG_OK;
@@ -222,7 +239,7 @@ int prepare_result(hbg_result *r, int64_t cap) {
         r->n_counters = 1 + 3 * nq + ng;
         CU(dalloc(&r->d_counters, r->n_counters));
         CU(cudaMallocHost((void **)&r->h_counters, r->n_counters * sizeof(unsigned long long)));
-        CU(dalloc(&r->d_tile, 1));
+        CU(dalloc(&r->d_tile, 2));
         for (auto &e : r->ev)
             CU(cudaEventCreate(&e));
     }
@@ -260,7 +277,7 @@ int enqueue_search(hbg_result *r) {
     const size_t nq = h.queries.size(), ng = h.groups.size();
     cudaStream_t st = r->stream;
     CU(cudaMemsetAsync(r->d_counters, 0, r->n_counters * sizeof(unsigned long long), st));
-    CU(cudaMemsetAsync(r->d_tile, 0, sizeof(unsigned int), st));
+    CU(cudaMemsetAsync(r->d_tile, 0, 2 * sizeof(unsigned int), st));
     if (r->d_gdiag)
         CU(cudaMemsetAsync(r->d_gdiag, 0, (size_t)r->gdiag_entries * sizeof(uint32_t), st));
 
@@ -274,6 +291,7 @@ int enqueue_search(hbg_result *r) {
     hbg_batch *b = r->batch;
     a.groups = b->d_groups;
     a.n_groups = (int32_t)ng;
+    a.group_list = b->d_group_list;
     a.cells = b->d_cells;
     a.entries = b->d_entries;
     a.pv = b->d_pv;
@@ -284,7 +302,7 @@ int enqueue_search(hbg_result *r) {
     a.window = h.window;
     a.tile_subjects = 128;
     a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
-    a.n_tiles = (int64_t)a.tiles_per_group * (int64_t)ng;
+    a.n_tiles = 0;
     a.tile_counter = r->d_tile;
     a.hsps = r->d_raw;
     a.hsp_count = r->d_counters;
@@ -305,7 +323,14 @@ int enqueue_search(hbg_result *r) {
         cap_status == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     CU(cudaEventRecordWithFlags(r->ev[0], st, ev_flags));
     if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
-        CU(hbg::launch_wordfinder(a, r->blocks, r->threads, st));
+        for (int mode = 0; mode < 2; ++mode) {
+            if (b->n_mode[mode] == 0)
+                continue;
+            a.group_list = b->d_group_list + (mode ? b->n_mode[0] : 0);
+            a.n_tiles = (int64_t)a.tiles_per_group * b->n_mode[mode];
+            a.tile_counter = r->d_tile + mode;
+            CU(hbg::launch_wordfinder(a, mode, r->blocks_mode[mode], r->threads, st));
+        }
     CU(cudaEventRecordWithFlags(r->ev[1], st, ev_flags));
 
     hbg::OrderArgs o;
@@ -328,7 +353,7 @@ int enqueue_search(hbg_result *r) {
     CU(hbg::launch_order(o, st));
     {
         const int bits = o.bits_q + o.bits_s + o.bits_so + o.bits_qo;
-        r->launches = (db->n > 0 ? 1 : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 2 + 3 * ((bits + 7) / 8) : 0) +
+        r->launches = (db->n > 0 ? (b->n_mode[0] > 0) + (b->n_mode[1] > 0) : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 2 + 3 * ((bits + 7) / 8) : 0) +
                       (nq > 0 ? 1 : 0);
     }
     CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
@@ -728,6 +753,7 @@ int hbg_batch_destroy(hbg_batch *b) {
         dfree(b->d_entries);
         dfree(b->d_pv);
         dfree(b->d_qcells);
+        dfree(b->d_group_list);
     }
     delete b;
     return HBG_OK;
@@ -823,15 +849,19 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
             delete r;
         return fail(HBG_ERR_CUDA, "cannot configure the word-finder kernel (wrong GPU?)");
     }
-    if (o.num_blocksx > 0) {
-        r->blocks = o.num_blocksx;
-    } else {
-        int sms = 1, per = 1;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
-        if (hbg::wordfinder_occupancy(r->threads, batch->host.smem_diag_len, &per) != cudaSuccess || per < 1)
-            per = 1;
-        r->blocks = sms * per;
+    for (int mode = 0; mode < 2; ++mode) {
+        if (o.num_blocksx > 0) {
+            r->blocks_mode[mode] = o.num_blocksx;
+        } else {
+            int sms = 1, per = 1;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
+            if (hbg::wordfinder_occupancy(mode, r->threads, batch->host.smem_diag_len, &per) != cudaSuccess ||
+                per < 1)
+                per = 1;
+            r->blocks_mode[mode] = sms * per;
+        }
     }
+    r->blocks = std::max(r->blocks_mode[0], r->blocks_mode[1]);
     if (cap == 0)
         cap = std::max<int64_t>(1 << 20, (int64_t)db->n);
     rc = prepare_result(r, std::max<int64_t>(cap, r->cap));
@@ -1076,13 +1106,16 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     if (hbg::wordfinder_smem_bytes(threads, h.smem_diag_len) > (size_t)optin)
         return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
     CU(hbg::wordfinder_configure());
-    int blocks = o.num_blocksx;
-    if (blocks <= 0) {
-        int sms = 1, per = 1;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
-        if (hbg::wordfinder_occupancy(threads, h.smem_diag_len, &per) != cudaSuccess || per < 1)
-            per = 1;
-        blocks = sms * per;
+    int blocks_mode[2];
+    for (int mode = 0; mode < 2; ++mode) {
+        blocks_mode[mode] = o.num_blocksx;
+        if (blocks_mode[mode] <= 0) {
+            int sms = 1, per = 1;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
+            if (hbg::wordfinder_occupancy(mode, threads, h.smem_diag_len, &per) != cudaSuccess || per < 1)
+                per = 1;
+            blocks_mode[mode] = sms * per;
+        }
     }
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *base = (unsigned char *)scratch;
@@ -1113,7 +1146,7 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     a.window = h.window;
     a.tile_subjects = 128;
     a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
-    a.n_tiles = (int64_t)a.tiles_per_group * ng;
+    a.n_tiles = 0;
     a.tile_counter = tile;
     a.hsps = d_hsps;
     a.hsp_count = d_counts;
@@ -1124,8 +1157,16 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     a.gdiag = nullptr;
     a.gdiag_len = 0;
     a.smem_diag = h.smem_diag_len;
-    if (db->n > 0)
-        CU(hbg::launch_wordfinder(a, blocks, threads, st));
+    if (db->n > 0) {
+        for (int mode = 0; mode < 2; ++mode) {
+            if (batch->n_mode[mode] == 0)
+                continue;
+            a.group_list = batch->d_group_list + (mode ? batch->n_mode[0] : 0);
+            a.n_tiles = (int64_t)a.tiles_per_group * batch->n_mode[mode];
+            a.tile_counter = tile + mode;
+            CU(hbg::launch_wordfinder(a, mode, blocks_mode[mode], threads, st));
+        }
+    }
     // per-query extension and kept counts follow the HSP count in d_counts
     CU(cudaMemcpyAsync(d_counts + 1, q_ext, sizeof(unsigned long long) * (size_t)(2 * nq),
                        cudaMemcpyDeviceToDevice, st));

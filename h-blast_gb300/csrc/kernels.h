@@ -19,6 +19,7 @@ struct WordFinderArgs {
     // batch
     const HbgGroup *groups;
     int32_t n_groups;
+    const int32_t *group_list;    // groups this launch processes (one hit mode per launch)
     const uint32_t *cells;        // n_groups x HBG_CELL_STRIDE
     const uint16_t *entries;
     const uint32_t *pv;           // n_groups x HBG_PV_WORDS
@@ -27,8 +28,8 @@ struct WordFinderArgs {
     const HbgContext *contexts;
     const HbgQueryDesc *queries;
     int32_t window;
-    // scheduling: tile t covers group t / tiles_per_group and scheduled
-    // subjects [(t % tiles_per_group) * tile_subjects, ... + tile_subjects)
+    // scheduling: tile t covers group group_list[t / tiles_per_group] and
+    // scheduled subjects [(t % tiles_per_group) * tile_subjects, + tile_subjects)
     int32_t tile_subjects;
     int32_t tiles_per_group;
     int64_t n_tiles;
@@ -51,8 +52,8 @@ struct WordFinderArgs {
 // Shared memory the word-finder kernel needs for a CTA of `threads` threads.
 size_t wordfinder_smem_bytes(int threads, int smem_diag);
 cudaError_t wordfinder_configure();
-cudaError_t wordfinder_occupancy(int threads, int smem_diag, int *blocks_per_sm);
-cudaError_t launch_wordfinder(const WordFinderArgs &a, int blocks, int threads,
+cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm);
+cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream);
 
 // Ordering pass: sort HSPs by (query, subject, s_off, q_off).

@@ -385,9 +385,16 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     restart_offset(it, diag_alloc);
     int n_tasks = 0, n_blk = 0, blk_cur = 0;
     unsigned long long item_hits = 0;
+    // software pipeline: the next chunk's cell bounds are loaded while this
+    // chunk's hits are applied, and each batch's query offsets while the
+    // previous batch is applied
+    uint32_t c_next = 0, base_next = 0;
+    if (it.S >= 3)
+        scan_words(it, sh, cs, 0, &c_next, &base_next);
     for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
-        uint32_t c, base;
-        scan_words(it, sh, cs, s0, &c, &base);
+        const uint32_t c = c_next, base = base_next;
+        if (s0 + 32 <= it.S - 3)
+            scan_words(it, sh, cs, s0 + 32, &c_next, &base_next);
         uint32_t incl = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -400,9 +407,9 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
         const uint32_t rel = base - excl;  // entry index of hit h = rel(owner) + h
         item_hits += T_;
 
-        for (uint32_t hb = 0; hb < T_; hb += 32) {
-            const uint32_t h = hb + lane;
-            const bool act = h < T_;
+        // hit h of the chunk: owner lane (largest lane whose exclusive count
+        // is <= h), its subject offset and its query offset
+        auto locate = [&](uint32_t h, int *s_h, int *q) {
             int lo = 0;
 #pragma unroll
             for (int step = 16; step > 0; step >>= 1) {
@@ -410,13 +417,19 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
                 if (v <= h)
                     lo += step;
             }
-            const int s_h = s0 + lo;
+            *s_h = s0 + lo;
             const uint32_t r = __shfl_sync(0xffffffffu, rel, lo);
-            int q = 0, d = 0;
-            if (act) {
-                q = __ldg(ents + (r + h));
-                d = (q - s_h) & it.mask;
-            }
+            *q = h < T_ ? (int)__ldg(ents + (r + h)) : 0;
+        };
+        int s_n = 0, q_n = 0;
+        if (T_ > 0)
+            locate((uint32_t)lane, &s_n, &q_n);
+        for (uint32_t hb = 0; hb < T_; hb += 32) {
+            const bool act = hb + lane < T_;
+            const int s_h = s_n, q = q_n;
+            if (hb + 32 < T_)
+                locate(hb + 32 + lane, &s_n, &q_n);
+            const int d = act ? ((q - s_h) & it.mask) : 0;
             apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
             // queues hold 64: keep room for one more batch of 32
             while (n_tasks >= 32 || n_blk >= 32)
@@ -428,7 +441,6 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     it.dofs += it.S + it.window;
     return item_hits;
 }
-
 
 // ---------------------------------------------------------------------------
 // Per-offset mode, for groups dense enough that one subject offset has many
@@ -537,7 +549,10 @@ __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFin
 
 }  // namespace
 
-__global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
+// Mode 0 (chunk mode) is built for four 256-thread CTAs per SM (64 registers
+// a thread), mode 1 (offset mode, large tables) for one.
+template <int Mode>
+__global__ void __launch_bounds__(256, Mode == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sh = *reinterpret_cast<Smem *>(smem_raw);
     const int lane = threadIdx.x & 31;
@@ -573,7 +588,7 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
         const long long tile = sh.tile;
         if (tile >= a.n_tiles)
             break;
-        const int g = (int)(tile / a.tiles_per_group);
+        const int g = a.group_list[tile / a.tiles_per_group];
         const int blk = (int)(tile % a.tiles_per_group);
         if (g != cur_group) {
             const uint32_t *src = a.pv + (size_t)g * HBG_PV_WORDS;
@@ -603,14 +618,14 @@ __global__ void __launch_bounds__(256) wordfinder_kernel(WordFinderArgs a) {
             if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = G.mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
-                              : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
+                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
+                            : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
                 dofs_s = it.dofs;
             } else {
                 Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = G.mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
-                              : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
+                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
+                            : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
                 dofs_g = it.dofs;
             }
             if (lane == 0)
@@ -637,17 +652,25 @@ cudaError_t wordfinder_configure() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return cudaFuncSetAttribute(wordfinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaError_t e = cudaFuncSetAttribute(wordfinder_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(wordfinder_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
 }
 
-cudaError_t wordfinder_occupancy(int threads, int smem_diag, int *blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel, threads,
-                                                         wordfinder_smem_bytes(threads, smem_diag));
+cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm) {
+    const size_t smem = wordfinder_smem_bytes(threads, smem_diag);
+    return mode ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
 }
 
-cudaError_t launch_wordfinder(const WordFinderArgs &a, int blocks, int threads,
+cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream) {
-    wordfinder_kernel<<<blocks, threads, wordfinder_smem_bytes(threads, a.smem_diag), stream>>>(a);
+    const size_t smem = wordfinder_smem_bytes(threads, a.smem_diag);
+    if (mode)
+        wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a);
+    else
+        wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -16,10 +16,13 @@ namespace hbg {
 // Shared-memory diagonal tables (16-bit cells) hold at most this many
 // entries per warp; groups whose table is longer use the global scratch.
 constexpr int32_t kSmemDiagMax = 16384;
-// Default group length: the table of a full group is 8192 entries (16 KB).
-constexpr int32_t kDefaultGroupTable = 8192;
-// Groups whose expected hits per subject offset reach this use offset mode.
-constexpr double kOffsetModeHits = 6.0;
+// Default group length: the table of a full group is 2048 entries (4 KB), small
+// enough for four 8-warp CTAs per SM.
+constexpr int32_t kDefaultGroupTable = 2048;
+// Groups whose expected hits per subject offset reach this use offset mode
+// (off by default: chunk mode at high occupancy measured faster; the autotuner
+// and hbg_batch_set_mode choose offset mode explicitly).
+constexpr double kOffsetModeHits = 1e30;
 // Queries per group are bounded so per-query counters fit in shared memory.
 constexpr int32_t kMaxQueriesPerGroup = 64;
 
