@@ -52,6 +52,87 @@ struct __align__(16) Smem {   // 16-byte size: the per-warp tables after it are 
 
 __device__ __forceinline__ int sc(const int8_t *m, int q, int s) { return m[q * 32 + s]; }
 
+// X-drop walk to the left from (s_off, q_off) inclusive; returns the best
+// score, *len = letters in the best walk.
+__device__ int extend_left(const int8_t *m, const uint8_t *s, const uint8_t *q, int s_off,
+                           int q_off, int dropoff, int *len) {
+    int n = min(s_off, q_off);
+    int best_i = n + 1;
+    int score = 0, maxscore = 0;
+    const uint8_t *sp = s + s_off - n;
+    const uint8_t *qp = q + q_off - n;
+    for (int i = n; i >= 0; --i) {
+        score += sc(m, qp[i], sp[i]);
+        if (score > maxscore) {
+            maxscore = score;
+            best_i = i;
+        }
+        if (maxscore - score >= dropoff)
+            break;
+    }
+    *len = n - best_i + 1;
+    return maxscore;
+}
+
+// X-drop walk to the right that also stops when the running score is <= 0.
+__device__ int extend_right(const int8_t *m, const uint8_t *s, int s_len, const uint8_t *q,
+                            int q_len, int s_off, int q_off, int dropoff, int maxscore,
+                            int *len, int *s_last_off) {
+    int n = min(s_len - s_off, q_len - q_off);
+    int best_i = -1;
+    int score = maxscore;
+    int i;
+    for (i = 0; i < n; ++i) {
+        score += sc(m, q[q_off + i], s[s_off + i]);
+        if (score > maxscore) {
+            maxscore = score;
+            best_i = i;
+        }
+        if (score <= 0 || maxscore - score >= dropoff)
+            break;
+    }
+    *len = best_i + 1;
+    *s_last_off = s_off + i;
+    return maxscore;
+}
+
+struct Ext {
+    int q_start, s_start, len, score, s_last_off;
+    bool right;
+};
+
+__device__ Ext extend_two_hit(const int8_t *m, const uint8_t *s, int s_len, const uint8_t *q,
+                              int q_len, int s_left_off, int s_right_off, int q_right_off,
+                              int dropoff) {
+    Ext e;
+    int right_d = 0, best = 0, acc = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        acc += sc(m, q[q_right_off + i], s[s_right_off + i]);
+        if (acc > best) {
+            best = acc;
+            right_d = i + 1;
+        }
+    }
+    q_right_off += right_d;
+    s_right_off += right_d;
+    int left_d = 0;
+    int left_score = extend_left(m, s, q, s_right_off - 1, q_right_off - 1, dropoff, &left_d);
+    int right_score = 0, rlen = 0;
+    e.s_last_off = s_right_off;
+    e.right = false;
+    if (left_d >= s_right_off - s_left_off) {
+        e.right = true;
+        right_score = extend_right(m, s, s_len, q, q_len, s_right_off, q_right_off, dropoff,
+                                   left_score, &rlen, &e.s_last_off);
+    }
+    e.q_start = q_right_off - left_d;
+    e.s_start = s_right_off - left_d;
+    e.len = left_d + rlen;
+    e.score = max(left_score, right_score);
+    return e;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned r;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
@@ -175,143 +256,6 @@ __device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d
     __syncwarp();
 }
 
-// Lockstep ungapped X-drop extensions (NCBI s_BlastAaExtendTwoHit / Left /
-// Right; H-BLAST h_blast_kernel.cu:1069-1540): end the word at its
-// best-scoring prefix; walk left from there, restarting the score at 0, until
-// the drop from the best reaches x_dropoff or the sequence start; if that
-// walk reached the first hit, walk right from the word end, starting at the
-// left score, until the score is <= 0, the drop reaches x_dropoff or a
-// sequence ends.  Every lane carries one queued extension and advances it one
-// letter per iteration; a lane whose walk ends writes its HSP and the
-// diagonal's new state and takes the next queued extension, so lanes stay
-// busy until the queue is empty.  Warp-collective.
-template <typename Cell>
-__device__ void run_tasks(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
-                          int n_tasks) {
-    using T = CellTraits<Cell>;
-    const int8_t *M = sh.matrix;
-    int next = 0;
-    int phase = 0;                 // 0 idle, 1 left walk, 2 right walk
-    int s_h = 0, ql = 0, s_r = 0, q_r = 0, s_left = 0;
-    const uint8_t *qs = it.gseq;   // the task's query, offset 0
-    int qlen = 0, cutoff = 0, xdrop = 0, query = 0, local = 0;
-    int i = 0, n = 0, score = 0, maxscore = 0, best = 0, left_d = 0, left_score = 0;
-    for (;;) {
-        const unsigned idle = __ballot_sync(0xffffffffu, phase == 0);
-        if (phase == 0) {
-            const int t = next + __popc(idle & lanemask_lt());
-            if (t < n_tasks) {
-                s_h = wq.task_s[t];
-                const int q = wq.task_q[t];
-                s_left = wq.task_left[t];
-                const HbgContext C = a.contexts[__ldg(it.gctx + q)];
-                const HbgQueryDesc Q = a.queries[C.query];
-                qs = it.gseq + Q.start;
-                qlen = Q.len;
-                ql = q - Q.start;
-                cutoff = C.cutoff;
-                xdrop = C.x_dropoff;
-                query = C.query;
-                local = C.local;
-                // end of the best-scoring prefix of the word
-                int right_d = 0, best3 = 0, acc = 0;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    acc += sc(M, qs[ql + k], it.s[s_h + k]);
-                    if (acc > best3) {
-                        best3 = acc;
-                        right_d = k + 1;
-                    }
-                }
-                q_r = ql + right_d;
-                s_r = s_h + right_d;
-                // left walk over (s_r - 1 - n + i, q_r - 1 - n + i), i = n .. 0
-                n = min(s_r - 1, q_r - 1);
-                i = n;
-                score = 0;
-                maxscore = 0;
-                best = n + 1;
-                phase = 1;
-            }
-        }
-        next += __popc(idle);
-        if (!__any_sync(0xffffffffu, phase != 0))
-            break;
-        bool done = false;         // walk finished this iteration
-        bool right = false;        // ... after a right walk
-        if (phase == 1) {
-            const int off = i - n - 1;
-            score += sc(M, qs[q_r + off], it.s[s_r + off]);
-            if (score > maxscore) {
-                maxscore = score;
-                best = i;
-            }
-            if (maxscore - score >= xdrop || i == 0) {
-                left_d = n - best + 1;
-                left_score = maxscore;
-                if (left_d >= s_r - s_left) {
-                    // the left walk reached the first hit: walk right from (s_r, q_r)
-                    n = min(it.S - s_r, qlen - q_r);
-                    i = 0;
-                    score = left_score;
-                    maxscore = left_score;
-                    best = -1;
-                    if (n > 0) {
-                        phase = 2;
-                    } else {
-                        done = true;
-                        right = true;
-                    }
-                } else {
-                    done = true;
-                }
-            } else {
-                --i;
-            }
-        } else if (phase == 2) {
-            score += sc(M, qs[q_r + i], it.s[s_r + i]);
-            if (score > maxscore) {
-                maxscore = score;
-                best = i;
-            }
-            if (score <= 0 || maxscore - score >= xdrop) {
-                done = true;
-                right = true;
-            } else if (++i == n) {
-                done = true;
-                right = true;
-            }
-        }
-        if (done) {
-            const int final_score = right ? maxscore : left_score;
-            const int len = left_d + (right ? best + 1 : 0);
-            atomicAdd(&sh.q_ext[query - it.first_query], 1u);
-            if (final_score >= cutoff) {
-                atomicAdd(&sh.q_kept[query - it.first_query], 1u);
-                const unsigned long long o = atomicAdd(a.hsp_count, 1ull);
-                if ((long long)o < a.hsp_cap) {
-                    hbg_hsp out;
-                    out.query = query;
-                    out.subject = it.j;
-                    out.q_start = q_r - left_d;
-                    out.s_start = s_r - left_d;
-                    out.q_off = ql;
-                    out.s_off = s_h;
-                    out.len = len;
-                    out.score = final_score;
-                    out.context = local;
-                    a.hsps[o] = out;
-                }
-            }
-            const int d = (ql + (int)(qs - it.gseq) - s_h) & it.mask;
-            it.diag[d] = right ? (Cell)(T::kFlag | (uint32_t)(s_r + i - 2 + it.dofs))
-                               : (Cell)(s_h + it.dofs);
-            phase = 0;
-        }
-    }
-    __syncwarp();
-}
-
 // One round: run every queued extension (lane per extension), then replay the
 // blocked hits once, in order.  Replayed hits may queue new extensions and be
 // blocked again behind them; that is safe mid-subject because every later hit
@@ -323,7 +267,39 @@ __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, W
     using T = CellTraits<Cell>;
     const int lane = threadIdx.x & 31;
     do {
-        run_tasks(it, a, sh, wq, n_tasks);
+        for (int t0 = 0; t0 < n_tasks; t0 += 32) {
+            const int i = t0 + lane;
+            if (i < n_tasks) {
+                const int s_h = wq.task_s[i], q = wq.task_q[i];
+                const int ci = __ldg(it.gctx + q);
+                const HbgContext C = a.contexts[ci];
+                const HbgQueryDesc Q = a.queries[C.query];
+                const int ql = q - Q.start;
+                const Ext e = extend_two_hit(sh.matrix, it.s, it.S, it.gseq + Q.start, Q.len,
+                                             wq.task_left[i], s_h, ql, C.x_dropoff);
+                atomicAdd(&sh.q_ext[C.query - it.first_query], 1u);
+                if (e.score >= C.cutoff) {
+                    atomicAdd(&sh.q_kept[C.query - it.first_query], 1u);
+                    const unsigned long long o = atomicAdd(a.hsp_count, 1ull);
+                    if ((long long)o < a.hsp_cap) {
+                        hbg_hsp out;
+                        out.query = C.query;
+                        out.subject = it.j;
+                        out.q_start = e.q_start;
+                        out.s_start = e.s_start;
+                        out.q_off = ql;
+                        out.s_off = s_h;
+                        out.len = e.len;
+                        out.score = e.score;
+                        out.context = C.local;
+                        a.hsps[o] = out;
+                    }
+                }
+                const int d = (q - s_h) & it.mask;
+                it.diag[d] = e.right ? (Cell)(T::kFlag | (uint32_t)(e.s_last_off - 2 + it.dofs))
+                                     : (Cell)(s_h + it.dofs);
+            }
+        }
         __syncwarp();
         n_tasks = 0;
         const int nb = n_blk;
