@@ -48,7 +48,9 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="hblast", choices=["hblast", "reference"])
-    p.add_argument("--config", default="batched", choices=["batched", "plain"])
+    p.add_argument("--config", default="batched", choices=["batched", "plain", "blastx", "served", "autotune"])
+    p.add_argument("--rates", default="2,5,10,20", help="served: Poisson arrival rates (queries/s)")
+    p.add_argument("--requests", type=int, default=60, help="served: requests per rate")
     p.add_argument("--subjects", type=int, default=0, help="override the database size (testing)")
     p.add_argument("--queries", type=int, default=0, help="override the number of queries (testing)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
@@ -60,8 +62,19 @@ def parse():
 
 # --------------------------------------------------------------------------- workload
 
+def frame_letters(nt_len: int) -> int:
+    """Letters of the six translated frames of a nucleotide query."""
+    return sum(max(nt_len - f % 3, 0) // 3 for f in range(6))
+
+
 def workload(cfg: str, rank: int, n_subjects: int, n_queries: int):
     from hblast import synth
+    if cfg == "blastx":
+        _, db = synth.batched_blastp(seed=rank, n_queries=64, n_subjects=n_subjects or 2_000_000)
+        nts = synth.blastx_queries(rank, db, n_queries=n_queries or 128)
+        desc = dict(workload="batched blastx: 128 nucleotide queries of 300..3000 nt (GC 0.5, planted ORFs matching "
+                             "database proteins at 40..70% identity), six frames, vs the 2,000,000-subject database")
+        return nts, db, desc
     if cfg == "plain":
         qs, db = synth.plain_blastp(seed=rank, n_subjects=n_subjects or 20000)
         desc = dict(workload="plain blastp: 1 query of 300 aa vs 20,000 lognormal subjects (median 300, "
@@ -185,6 +198,112 @@ def reference_arm(args):
     }), flush=True)
 
 
+# --------------------------------------------------------------------------- served and autotune
+
+def served_arm(args):
+    """Poisson arrivals of 80% BLASTP (lognormal median 350, sigma 1.0, 30..35,000 aa) and 20% BLASTX
+    (300..3000 nt) against a resident database; p50/p99 latency per rate, for the continuous-batching
+    server and for the plain form (one query per launch, one at a time)."""
+    import threading
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as g
+    g.build()
+    import hblast
+    from hblast import synth
+    n_sub = args.subjects or 10_000_000
+    rng = np.random.default_rng(0)
+    db = synth.make_db(rng, n_sub, 300, 0.6, 30, 5000, 0.01, [synth.random_letters(rng, 400)],
+                       lambda r: r.integers(50, 301), lambda r: r.uniform(0.3, 0.6))
+    gdb = hblast.Database(db.residues, db.offsets)
+    ssum = int(db.offsets[-1])
+    xd6, cu6 = np.full(6, 16, np.int32), np.full(6, 41, np.int32)
+    out = {"metric": "served latency", "config": {"workload": f"served mixed stream vs {n_sub} subjects "
+                                                               f"({ssum} residues)", "requests_per_rate": args.requests}}
+    rates = [float(x) for x in args.rates.split(",")]
+    for form in ("served", "plain"):
+        res_form = []
+        for rate in rates:
+            r = np.random.default_rng(int(rate * 1000) + 7)
+            kinds = r.random(args.requests) < 0.8
+            lens = synth.lognormal_lengths(r, args.requests, 350, 1.0, 30, 35000)
+            reqs = []
+            for k, L in zip(kinds, lens):
+                if k:
+                    reqs.append(("p", synth.random_letters(r, int(L))))
+                else:
+                    reqs.append(("x", r.integers(0, 4, size=int(r.integers(300, 3001))).astype(np.uint8)))
+            gaps = r.exponential(1.0 / rate, size=args.requests)
+            so = dict(max_inflight=2, max_batch_queries=512) if form == "served" else \
+                dict(max_inflight=1, max_batch_queries=1)
+            srv = hblast.Server(gdb, **so)
+            tickets = []
+            letters = 0
+            t_start = time.perf_counter()
+
+            def produce():
+                nonlocal letters
+                t = time.perf_counter()
+                for (kind, seq), gap in zip(reqs, gaps):
+                    t += gap
+                    d = t - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    if kind == "p":
+                        tickets.append(srv.submit(hblast.ProteinQuery.blastp(seq)))
+                        letters += len(seq)
+                    else:
+                        tickets.append(srv.submit_blastx(seq, xd6, cu6))
+                        letters += frame_letters(len(seq))
+
+            th = threading.Thread(target=produce)
+            th.start()
+            th.join()
+            lat = []
+            for t in tickets:
+                _, _, ms = srv.take(t)
+                lat.append(ms)
+            wall = time.perf_counter() - t_start
+            c = srv.counters()
+            srv.close()
+            lat = np.array(lat)
+            res_form.append({"rate": rate, "p50_ms": float(np.percentile(lat, 50)),
+                             "p99_ms": float(np.percentile(lat, 99)), "wall_s": wall,
+                             "queries_per_s": len(lat) / wall, "residues_per_s": letters * ssum / wall,
+                             "batches": c["batches"], "largest_batch": c["largest_batch"]})
+            print(json.dumps({"form": form, **res_form[-1]}), file=sys.stderr, flush=True)
+        out[form] = res_form
+    print(json.dumps(out), flush=True)
+
+
+def autotune_arm(args):
+    """Config-4 sweep: batches of 1, 8, 64 and 512 heavy-tailed queries (lognormal median 350,
+    sigma 1.0, 30..35,000 aa) against a database sample; per length bucket the tuner's choice and
+    the achieved subject-stream GB/s of every candidate."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as g
+    g.build()
+    import hblast
+    from hblast import autotune, synth
+    n_sub = args.subjects or 500_000
+    rng = np.random.default_rng(0)
+    db = synth.make_db(rng, n_sub, 300, 0.6, 30, 5000, 0.01, [synth.random_letters(rng, 400)],
+                       lambda r: r.integers(50, 301), lambda r: r.uniform(0.3, 0.6))
+    gdb = hblast.Database(db.residues, db.offsets)
+    ssum = int(db.offsets[-1])
+    report = {"metric": "autotune", "config": {"workload": f"heavy-tailed batches vs {n_sub} subjects ({ssum} residues)"}}
+    for nb in (1, 8, 64, 512):
+        qs = synth.heavy_tailed_queries(nb, nb)
+        pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+        table = autotune.tune(gdb, pqs, ssum, reps=1)
+        report[f"batch_{nb}"] = [{"bucket": [t.lo, t.hi], "n_queries": t.n_queries,
+                                  "best": None if t.best is None else t.best.__dict__,
+                                  "rows": t.rows} for t in table]
+        print(json.dumps({"batch": nb, "buckets": report[f"batch_{nb}"]}), file=sys.stderr, flush=True)
+    print(json.dumps(report), flush=True)
+
+
 # --------------------------------------------------------------------------- GPU arm
 
 def main():
@@ -192,6 +311,12 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.config == "served":
+        served_arm(args)
+        return
+    if args.config == "autotune":
+        autotune_arm(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -209,13 +334,26 @@ def main():
     import hblast
 
     qs, db, desc = workload(args.config, rank, args.subjects, args.queries)
-    qsum = int(sum(len(q) for q in qs))
+    blastx = args.config == "blastx"
+    qsum = int(sum(frame_letters(len(q)) if blastx else len(q) for q in qs))
     ssum = int(db.offsets[-1])
     units_per_step = float(qsum) * float(ssum)
     opts = hblast.default_options(method=0)
     gdb = hblast.Database(db.residues, db.offsets, opts)
-    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
-    batch = hblast.Batch.proteins(pqs)
+    if blastx:
+        xd6 = np.full((1, 6), 16, np.int32)
+        cu6 = np.full((1, 6), 41, np.int32)
+        pqs = list(qs)
+
+        def batch_of(specs, max_group_len=0):
+            n = len(specs)
+            return hblast.Batch.blastx(specs, np.repeat(xd6, n, 0), np.repeat(cu6, n, 0), max_group_len=max_group_len)
+    else:
+        pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+
+        def batch_of(specs, max_group_len=0):
+            return hblast.Batch.proteins(specs, max_group_len=max_group_len)
+    batch = batch_of(pqs)
     binfo = batch.info()
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
@@ -291,8 +429,8 @@ def main():
 
     # one-query-per-launch form (the plain GPU form) on the same database
     plain = None
-    if not args.no_plain and args.config == "batched":
-        single = [hblast.Batch.proteins([p]) for p in pqs]
+    if not args.no_plain and args.config in ("batched", "blastx"):
+        single = [batch_of([p]) for p in pqs]
         sss = [hblast.Searcher(gdb, b1, opts) for b1 in single]
         for x in sss:
             x.launch(sptr)
@@ -307,7 +445,7 @@ def main():
         torch.cuda.synchronize()
         tp = (time.perf_counter() - t0) / reps
         plain = {"value": units_per_step * world / tp, "unit": UNIT, "ms_per_step": tp * 1e3,
-                 "form": "64 launches, one query each, same database"}
+                 "form": f"{len(pqs)} launches, one query each, same database"}
         for x in sss:
             x.close()
         for b1 in single:
@@ -321,7 +459,7 @@ def main():
         for i in range(1 + max(1, args.steps // 3)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            b2 = hblast.Batch.proteins(pqs)
+            b2 = batch_of(pqs)
             r2 = hblast.search(gdb, b2, opts, hsp_capacity=max(int(n_hsps * 1.1) + 1024, 1 << 20), stream=sptr)
             h2d = b2.info()["device_bytes"]
             b2.close()
@@ -335,7 +473,7 @@ def main():
                "path": "hbg_batch_create (host lookup tables) + hbg_search + hbg_result_wait"}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not blastx:
         threads = os.cpu_count() or 1
         v, t, n, r = cpu_sample_search(qs, db, args.cpu_seconds, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",

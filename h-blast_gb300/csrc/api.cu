@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <numeric>
@@ -77,7 +78,13 @@ struct DeviceScope {
 
 }  // namespace
 
+// Databases and batches carry a process-unique id: a new object can reuse a
+// freed one's address, so reuse checks and graph keys compare ids, never
+// pointers.
+static std::atomic<uint64_t> g_next_object_id{1};
+
 struct hbg_db {
+    uint64_t id = g_next_object_id++;
     int device = 0;
     int32_t n = 0;
     int64_t n_res = 0;
@@ -92,6 +99,7 @@ struct hbg_db {
 };
 
 struct hbg_batch {
+    uint64_t id = g_next_object_id++;
     hbg::HostBatch host;
     int device = -1;
     HbgGroup *d_groups = nullptr;
@@ -141,7 +149,8 @@ struct hbg_result {
     int32_t launches = 0;   // kernels per search
     int64_t launch_count = 0;
     cudaGraphExec_t graph_exec = nullptr;
-    long long graph_key[5] = {0, 0, 0, 0, 0};
+    uint64_t db_id = 0, batch_id = 0;   // what the buffers were last prepared for
+    long long graph_key[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -235,13 +244,19 @@ void free_result_device(hbg_result *r) {
 int prepare_result(hbg_result *r, int64_t cap) {
     const hbg::HostBatch &h = r->batch->host;
     const size_t nq = h.queries.size(), ng = h.groups.size();
-    if (!r->d_counters) {
-        r->n_counters = 1 + 3 * nq + ng;
-        CU(dalloc(&r->d_counters, r->n_counters));
-        CU(cudaMallocHost((void **)&r->h_counters, r->n_counters * sizeof(unsigned long long)));
+    if (!r->d_tile) {
         CU(dalloc(&r->d_tile, 2));
         for (auto &e : r->ev)
             CU(cudaEventCreate(&e));
+    }
+    if (r->n_counters < 1 + 3 * nq + ng) {   // first use, or a larger batch
+        dfree(r->d_counters);
+        if (r->h_counters)
+            cudaFreeHost(r->h_counters);
+        r->h_counters = nullptr;
+        r->n_counters = 1 + 3 * nq + ng;
+        CU(dalloc(&r->d_counters, r->n_counters));
+        CU(cudaMallocHost((void **)&r->h_counters, r->n_counters * sizeof(unsigned long long)));
     }
     r->gdiag_len = global_diag_len(h, r->db);
     if (r->gdiag_len > 0) {
@@ -375,7 +390,8 @@ void drop_graph(hbg_result *r) {
 int launch_search(hbg_result *r) {
     CU(hbg::wordfinder_configure());
     const bool graphable = r->stream != nullptr && r->launch_count > 0;
-    const long long key[5] = {(long long)r->cap, r->blocks, r->threads, (long long)r->gdiag_entries,
+    const long long key[6] = {(long long)r->batch_id, (long long)r->cap, r->blocks, r->threads,
+                              (long long)r->gdiag_entries,
                               (long long)(uintptr_t)r->stream};
     if (!graphable) {
         int rc = enqueue_search(r);
@@ -816,15 +832,26 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
     if (rc != HBG_OK)
         return rc;
     hbg_result *r = *out;
-    if (r && (r->db != db || r->batch != batch)) {
-        return fail(HBG_ERR_STATE, "a reused result must belong to the same database and batch");
+    if (r && (r->db != db || r->db_id != db->id))
+        return fail(HBG_ERR_STATE, "a reused result must belong to the same database");
+    if (r && r->launched && !r->synced)
+        return fail(HBG_ERR_STATE, "the result's previous search has not been waited for");
+    if (r && (r->batch != batch || r->batch_id != batch->id)) {
+        // re-target the buffers to another batch of the same database
+        r->batch = batch;
+        r->batch_id = batch->id;
+        r->graph_exec ? (void)cudaGraphExecDestroy(r->graph_exec) : (void)0;
+        r->graph_exec = nullptr;
+        r->launch_count = 0;
     }
     if (!r) {
         r = new (std::nothrow) hbg_result;
         if (!r)
             return fail(HBG_ERR_NOMEM, "host allocation");
         r->db = db;
+        r->db_id = db->id;
         r->batch = batch;
+        r->batch_id = batch->id;
         r->device = db->device;
     }
     r->opt = o;

@@ -55,6 +55,12 @@ class RuntimeOptions(C.Structure):
                 ("load_factor", C.c_int32), ("chunk_size", C.c_int32), ("base_value", C.c_int32)]
 
 
+class ServerOptions(C.Structure):
+    """hbg_server_options: slots in flight, queries per batch, memory budget, group length."""
+    _fields_ = [("max_inflight", C.c_int32), ("max_batch_queries", C.c_int32), ("memory_budget", C.c_int64),
+                ("max_group_len", C.c_int32), ("pad", C.c_int32)]
+
+
 class QueryStats(C.Structure):
     _fields_ = [("lookup_hits", C.c_int64), ("init_extends", C.c_int64), ("good_init_extends", C.c_int64),
                 ("subjects_passed", C.c_int64)]
@@ -95,6 +101,15 @@ _SIGS = {
     "hbg_search_sync": ([_P, _P, C.POINTER(GpuOptions), _P, C.c_int64, C.POINTER(C.c_int64),
                          C.POINTER(QueryStats), _P], C.c_int),
     "hbg_search_static": ([_P, _P, C.POINTER(GpuOptions), _P, C.c_int64, _P, _P], C.c_int),
+    "hbg_server_default_options": ([C.c_void_p], C.c_int),
+    "hbg_server_create": ([_P, C.POINTER(_WordParams), C.POINTER(GpuOptions), C.c_void_p, C.POINTER(_P)], C.c_int),
+    "hbg_server_submit": ([_P, C.POINTER(_Query), C.POINTER(C.c_int64)], C.c_int),
+    "hbg_server_submit_blastx": ([_P, _P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int64)], C.c_int),
+    "hbg_server_wait": ([_P, C.c_int64, C.c_int32, C.POINTER(C.c_int64)], C.c_int),
+    "hbg_server_take": ([_P, C.c_int64, _P, C.c_int64, C.POINTER(QueryStats), C.POINTER(C.c_double)], C.c_int),
+    "hbg_server_counters": ([_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
+    "hbg_server_destroy": ([_P], C.c_int),
 }
 
 _lib = None
@@ -360,6 +375,76 @@ class Searcher:
         if self.res:
             _check(lib().hbg_result_free(self.res))
             self.res = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop over a resident database (hbg_server_*)."""
+
+    def __init__(self, db: Database, threshold: int = 11, window: int = 40, options: GpuOptions | None = None,
+                 **server_options):
+        so = ServerOptions()
+        _check(lib().hbg_server_default_options(C.byref(so)))
+        for k, v in server_options.items():
+            setattr(so, k, v)
+        wp = _WordParams(threshold, window)
+        h = C.c_void_p()
+        _check(lib().hbg_server_create(db.handle, C.byref(wp), C.byref(options) if options is not None else None,
+                                       C.byref(so), C.byref(h)))
+        self.handle = h
+        self.db = db
+
+    def submit(self, q: ProteinQuery) -> int:
+        seq = np.ascontiguousarray(q.sequence, dtype=np.uint8)
+        co = np.ascontiguousarray(q.context_offset, dtype=np.int32)
+        cl = np.ascontiguousarray(q.context_length, dtype=np.int32)
+        xd = np.ascontiguousarray(q.x_dropoff, dtype=np.int32)
+        cu = np.ascontiguousarray(q.cutoff_score, dtype=np.int32)
+        cq = _Query(seq.ctypes.data_as(C.POINTER(C.c_uint8)), q.length, len(co), _i32p(co), _i32p(cl), _i32p(xd),
+                    _i32p(cu))
+        t = C.c_int64()
+        _check(lib().hbg_server_submit(self.handle, C.byref(cq), C.byref(t)))
+        return t.value
+
+    def submit_blastx(self, nt: np.ndarray, x_dropoff, cutoff) -> int:
+        nt = np.ascontiguousarray(nt, dtype=np.uint8)
+        xd = np.ascontiguousarray(x_dropoff, dtype=np.int32)
+        cu = np.ascontiguousarray(cutoff, dtype=np.int32)
+        t = C.c_int64()
+        _check(lib().hbg_server_submit_blastx(self.handle, nt.ctypes.data, len(nt), _i32p(xd), _i32p(cu),
+                                              C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> int:
+        n = C.c_int64()
+        _check(lib().hbg_server_wait(self.handle, ticket, timeout_ms, C.byref(n)))
+        return n.value
+
+    def take(self, ticket: int):
+        """(hsps, stats dict, latency ms) of a finished request."""
+        n = self.wait(ticket)
+        out = np.zeros(n, dtype=HSP_DTYPE)
+        st = QueryStats()
+        lat = C.c_double()
+        _check(lib().hbg_server_take(self.handle, ticket, out.ctypes.data if n else None, n, C.byref(st),
+                                     C.byref(lat)))
+        return out, dict(lookup_hits=st.lookup_hits, init_extends=st.init_extends,
+                         good_init_extends=st.good_init_extends, subjects_passed=st.subjects_passed), lat.value
+
+    def counters(self):
+        b, q, l = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().hbg_server_counters(self.handle, C.byref(b), C.byref(q), C.byref(l)))
+        return dict(batches=b.value, queries=q.value, largest_batch=l.value)
+
+    def close(self):
+        if self.handle:
+            _check(lib().hbg_server_destroy(self.handle))
+            self.handle = None
 
     def __del__(self):
         try:

@@ -230,7 +230,10 @@ int hbg_mem_required(const hbg_db *db, const hbg_batch *batch, int64_t hsp_capac
  * one slot per subject, at least 1 Mi; H-BLAST sizes it as AVG_HSPS_PER_SEQUENCE
  * slots per subject, NF/functions.cpp:1513-1516);
  * if a search finds more, hbg_result_wait relaunches it once with a buffer of
- * the exact size, so results never depend on the capacity. */
+ * the exact size, so results never depend on the capacity.  *out == NULL
+ * creates a result; a result from an earlier search of the same database may
+ * be passed back (after it was waited for) to reuse its buffers, with the
+ * same or another batch. */
 int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt,
                int64_t hsp_capacity, void *stream, hbg_result **out);
 
@@ -264,6 +267,55 @@ int hbg_result_stats(const hbg_result *res, int32_t q, hbg_query_stats *out);
 /* Release device and host buffers (replaces H_BLAST_free_memory,
  * h_blast.cu:1254-1278). */
 int hbg_result_free(hbg_result *res);
+
+/* ---- serving ---------------------------------------------------------------- */
+
+/* A request loop over a resident database: queries submitted from any thread
+ * are admitted in arrival order while device memory for their lookup tables
+ * and HSP buffers stays within memory_budget, packed into batches as they
+ * arrive, and searched with up to max_inflight searches on the GPU at once
+ * (continuous batching: a batch is formed whenever a slot frees).  Each
+ * query's HSPs are the same as searching it alone.  Replaces the CPU/GPU load
+ * balancer and the multi-process query split of H-BLAST
+ * (NF/functions.cpp:51-140,1221-1827; scripts/H-BLASTM:212-305). */
+typedef struct hbg_server hbg_server;
+
+typedef struct hbg_server_options {
+    int32_t max_inflight;        /* searches in flight (default 2) */
+    int32_t max_batch_queries;   /* queries per batch (default 512) */
+    int64_t memory_budget;       /* device bytes for in-flight batches (default 32 GiB) */
+    int32_t max_group_len;       /* 0 = library default */
+    int32_t pad;
+} hbg_server_options;
+
+int hbg_server_default_options(hbg_server_options *opt);
+int hbg_server_create(hbg_db *db, const hbg_word_params *params, const hbg_gpu_options *opt,
+                      const hbg_server_options *sopt, hbg_server **out);
+
+/* Submit one protein query (any number of contexts); *ticket identifies it. */
+int hbg_server_submit(hbg_server *s, const hbg_query *query, int64_t *ticket);
+
+/* Submit one nucleotide query for BLASTX (six frames, per-frame x_dropoff and
+ * cutoff_score, 6 values each). */
+int hbg_server_submit_blastx(hbg_server *s, const uint8_t *nt, int32_t nt_len,
+                             const int32_t *x_dropoff, const int32_t *cutoff_score,
+                             int64_t *ticket);
+
+/* Wait up to timeout_ms (< 0 = forever) for a request; HBG_ERR_STATE if it is
+ * not done in time.  *n_hsps receives its HSP count. */
+int hbg_server_wait(hbg_server *s, int64_t ticket, int32_t timeout_ms, int64_t *n_hsps);
+
+/* Copy a finished request's HSPs (query field 0; reference order) and stats,
+ * its latency from submission to completion, then forget the request. */
+int hbg_server_take(hbg_server *s, int64_t ticket, hbg_hsp *out, int64_t cap,
+                    hbg_query_stats *stats, double *latency_ms);
+
+/* Totals since creation: batches launched, queries completed, largest batch. */
+int hbg_server_counters(const hbg_server *s, int64_t *batches, int64_t *queries,
+                        int64_t *largest_batch);
+
+/* Finish every admitted request, then stop. */
+int hbg_server_destroy(hbg_server *s);
 
 /* ---- search without allocation -------------------------------------------- */
 
