@@ -83,6 +83,21 @@ struct DeviceScope {
 // pointers.
 static std::atomic<uint64_t> g_next_object_id{1};
 
+// Groups are searched in launch classes: one hit mode and one shared-table
+// size per launch, so a long query's large table does not cut the occupancy
+// of every other group in its batch.
+struct LaunchClass {
+    int mode;        // 0 chunk mode, 1 offset mode
+    int smem_diag;   // per-warp 16-bit table entries (small for the global class)
+    int first;       // groups [first, first + count) of the batch's group list
+    int count;
+};
+struct LaunchShape {
+    int threads;
+    int blocks;
+};
+constexpr int kMaxLaunchClasses = 16;
+
 struct hbg_db {
     uint64_t id = g_next_object_id++;
     int device = 0;
@@ -111,8 +126,8 @@ struct hbg_batch {
     uint16_t *d_entries = nullptr;
     uint32_t *d_pv = nullptr;
     uint16_t *d_qcells = nullptr;
-    int32_t *d_group_list = nullptr;   // chunk-mode groups, then offset-mode groups
-    int32_t n_mode[2] = {0, 0};
+    int32_t *d_group_list = nullptr;   // groups ordered by launch class
+    std::vector<LaunchClass> classes;
     int64_t device_bytes = 0;
 };
 
@@ -123,8 +138,9 @@ struct hbg_result {
     cudaStream_t stream = nullptr;
     int device = 0;
     int64_t cap = 0;
-    int blocks = 0, threads = 256;   // blocks = the larger of the two modes' grids
-    int blocks_mode[2] = {0, 0};
+    int blocks = 0, threads = 256;   // the largest grid and CTA over launch classes
+    std::vector<LaunchShape> shapes; // one per launch class of the batch
+    hbg_gpu_options shape_opt{};     // options the shapes were computed for
     // device
     hbg_hsp *d_raw = nullptr, *d_sorted = nullptr;
     unsigned long long *d_counters = nullptr;  // [0]=hsp count, then per query ext, kept, hits; per group hits
@@ -189,16 +205,27 @@ int upload_batch(hbg_batch *b, int device) {
     CU(cudaMemcpy(b->d_pv, h.pv.data(), h.pv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_qcells, h.query_cells.data(), h.query_cells.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     {
-        // one launch per hit mode: list the groups of each mode
-        std::vector<int32_t> list;
-        for (int mode = 0; mode < 2; ++mode) {
-            b->n_mode[mode] = 0;
-            for (int32_t g = 0; g < (int32_t)h.groups.size(); ++g)
-                if (h.groups[g].mode == mode) {
-                    list.push_back(g);
-                    b->n_mode[mode]++;
-                }
+        // launch classes: (mode, table size); tables of <= 2048 entries share
+        // one class (they all allow four CTAs per SM); global-table groups
+        // form their own class per mode
+        std::vector<std::pair<std::pair<int, int>, int32_t>> keyed;
+        for (int32_t g = 0; g < (int32_t)h.groups.size(); ++g) {
+            const HbgGroup &G = h.groups[g];
+            const int size = G.placement ? 64 : std::max<int>(2048, G.diag_len);
+            keyed.push_back({{G.mode, size}, g});
         }
+        std::stable_sort(keyed.begin(), keyed.end(),
+                         [](const auto &x, const auto &y) { return x.first < y.first; });
+        std::vector<int32_t> list;
+        b->classes.clear();
+        for (size_t i = 0; i < keyed.size(); ++i) {
+            if (i == 0 || keyed[i].first != keyed[i - 1].first)
+                b->classes.push_back(LaunchClass{keyed[i].first.first, keyed[i].first.second, (int)i, 0});
+            b->classes.back().count++;
+            list.push_back(keyed[i].second);
+        }
+        if ((int)b->classes.size() > kMaxLaunchClasses)
+            return fail(HBG_ERR_INVALID, "too many launch classes");
         CU(dalloc(&b->d_group_list, list.size()));
         CU(cudaMemcpy(b->d_group_list, list.data(), list.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     }
@@ -215,6 +242,32 @@ int32_t global_diag_len(const hbg::HostBatch &h, const hbg_db *db) {
     if (db->max_len + h.window > 0x7fff)
         len = std::max<int32_t>(len, h.smem_diag_len);
     return len;
+}
+
+// CTA size and grid of each launch class: the CTA is halved until its
+// per-warp tables fit the shared-memory carve-out; the grid is one wave at
+// the occupancy that leaves (or the caller's num_blocksx).
+int plan_launches(const hbg_batch *b, const hbg_gpu_options &o, int device, std::vector<LaunchShape> *out) {
+    int optin = 0, sms = 1;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    out->clear();
+    for (const LaunchClass &lc : b->classes) {
+        int t = o.num_threadsx;
+        while (t > 32 && hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
+            t = ((t / 2) + 31) / 32 * 32;
+        if (hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
+            return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
+        int blocks = o.num_blocksx;
+        if (blocks <= 0) {
+            int per = 1;
+            if (hbg::wordfinder_occupancy(lc.mode, t, lc.smem_diag, &per) != cudaSuccess || per < 1)
+                per = 1;
+            blocks = sms * per;
+        }
+        out->push_back(LaunchShape{t, blocks});
+    }
+    return HBG_OK;
 }
 
 void free_result_device(hbg_result *r) {
@@ -245,7 +298,7 @@ int prepare_result(hbg_result *r, int64_t cap) {
     const hbg::HostBatch &h = r->batch->host;
     const size_t nq = h.queries.size(), ng = h.groups.size();
     if (!r->d_tile) {
-        CU(dalloc(&r->d_tile, 2));
+        CU(dalloc(&r->d_tile, kMaxLaunchClasses));
         for (auto &e : r->ev)
             CU(cudaEventCreate(&e));
     }
@@ -292,7 +345,7 @@ int enqueue_search(hbg_result *r) {
     const size_t nq = h.queries.size(), ng = h.groups.size();
     cudaStream_t st = r->stream;
     CU(cudaMemsetAsync(r->d_counters, 0, r->n_counters * sizeof(unsigned long long), st));
-    CU(cudaMemsetAsync(r->d_tile, 0, 2 * sizeof(unsigned int), st));
+    CU(cudaMemsetAsync(r->d_tile, 0, kMaxLaunchClasses * sizeof(unsigned int), st));
     if (r->d_gdiag)
         CU(cudaMemsetAsync(r->d_gdiag, 0, (size_t)r->gdiag_entries * sizeof(uint32_t), st));
 
@@ -338,13 +391,13 @@ int enqueue_search(hbg_result *r) {
         cap_status == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     CU(cudaEventRecordWithFlags(r->ev[0], st, ev_flags));
     if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
-        for (int mode = 0; mode < 2; ++mode) {
-            if (b->n_mode[mode] == 0)
-                continue;
-            a.group_list = b->d_group_list + (mode ? b->n_mode[0] : 0);
-            a.n_tiles = (int64_t)a.tiles_per_group * b->n_mode[mode];
-            a.tile_counter = r->d_tile + mode;
-            CU(hbg::launch_wordfinder(a, mode, r->blocks_mode[mode], r->threads, st));
+        for (size_t c = 0; c < b->classes.size(); ++c) {
+            const LaunchClass &lc = b->classes[c];
+            a.group_list = b->d_group_list + lc.first;
+            a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
+            a.tile_counter = r->d_tile + c;
+            a.smem_diag = lc.smem_diag;
+            CU(hbg::launch_wordfinder(a, lc.mode, r->shapes[c].blocks, r->shapes[c].threads, st));
         }
     CU(cudaEventRecordWithFlags(r->ev[1], st, ev_flags));
 
@@ -368,7 +421,7 @@ int enqueue_search(hbg_result *r) {
     CU(hbg::launch_order(o, st));
     {
         const int bits = o.bits_q + o.bits_s + o.bits_so + o.bits_qo;
-        r->launches = (db->n > 0 ? (b->n_mode[0] > 0) + (b->n_mode[1] > 0) : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 2 + 3 * ((bits + 7) / 8) : 0) +
+        r->launches = (db->n > 0 ? (int32_t)b->classes.size() : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 2 + 3 * ((bits + 7) / 8) : 0) +
                       (nq > 0 ? 1 : 0);
     }
     CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
@@ -390,8 +443,9 @@ void drop_graph(hbg_result *r) {
 int launch_search(hbg_result *r) {
     CU(hbg::wordfinder_configure());
     const bool graphable = r->stream != nullptr && r->launch_count > 0;
-    const long long key[6] = {(long long)r->batch_id, (long long)r->cap, r->blocks, r->threads,
-                              (long long)r->gdiag_entries,
+    const long long key[6] = {(long long)r->batch_id, (long long)r->cap,
+                              ((long long)r->shape_opt.num_blocksx << 32) | (unsigned)r->shape_opt.num_threadsx,
+                              r->blocks, (long long)r->gdiag_entries,
                               (long long)(uintptr_t)r->stream};
     if (!graphable) {
         int rc = enqueue_search(r);
@@ -856,39 +910,24 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
     }
     r->opt = o;
     r->stream = (cudaStream_t)stream;
-    // a CTA's per-warp shared tables must fit the shared-memory carve-out:
-    // halve the CTA until they do (large groups get fewer warps per CTA)
-    {
-        int optin = 0;
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, db->device);
-        int t = o.num_threadsx;
-        while (t > 32 && hbg::wordfinder_smem_bytes(t, batch->host.smem_diag_len) > (size_t)optin)
-            t = ((t / 2) + 31) / 32 * 32;
-        if (hbg::wordfinder_smem_bytes(t, batch->host.smem_diag_len) > (size_t)optin) {
-            if (!*out)
-                delete r;
-            return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
-        }
-        r->threads = t;
-    }
     if (hbg::wordfinder_configure() != cudaSuccess) {
         if (!*out)
             delete r;
         return fail(HBG_ERR_CUDA, "cannot configure the word-finder kernel (wrong GPU?)");
     }
-    for (int mode = 0; mode < 2; ++mode) {
-        if (o.num_blocksx > 0) {
-            r->blocks_mode[mode] = o.num_blocksx;
-        } else {
-            int sms = 1, per = 1;
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
-            if (hbg::wordfinder_occupancy(mode, r->threads, batch->host.smem_diag_len, &per) != cudaSuccess ||
-                per < 1)
-                per = 1;
-            r->blocks_mode[mode] = sms * per;
-        }
+    rc = plan_launches(batch, o, db->device, &r->shapes);
+    if (rc != HBG_OK) {
+        if (!*out)
+            delete r;
+        return rc;
     }
-    r->blocks = std::max(r->blocks_mode[0], r->blocks_mode[1]);
+    r->shape_opt = o;
+    r->blocks = 0;
+    r->threads = 32;
+    for (const LaunchShape &sh : r->shapes) {
+        r->blocks = std::max(r->blocks, sh.blocks);
+        r->threads = std::max(r->threads, sh.threads);
+    }
     if (cap == 0)
         cap = std::max<int64_t>(1 << 20, (int64_t)db->n);
     rc = prepare_result(r, std::max<int64_t>(cap, r->cap));
@@ -1112,7 +1151,8 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
         return fail(HBG_ERR_INVALID, "num_threadsx must be a multiple of 32 in 32..256");
     const hbg::HostBatch &h = batch->host;
     const int64_t nq = (int64_t)h.queries.size(), ng = (int64_t)h.groups.size();
-    // scratch layout: [tile counter | per-query extensions | per-query kept | per-group hits]
+    // scratch layout: [tile counters (one per launch class) | per-query extensions |
+    //                  per-query kept | per-group hits]
     const int64_t need = 256 + 8 * (2 * nq + ng);
     if (need > HBG_STATIC_SCRATCH_BYTES)
         return fail(HBG_ERR_TOO_LONG, "hbg_search_static: the batch needs " + std::to_string(need) +
@@ -1125,25 +1165,11 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     int rc = static_scratch(db->device, &scratch);
     if (rc != HBG_OK)
         return rc;
-    int optin = 0;
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, db->device);
-    int threads = o.num_threadsx;
-    while (threads > 32 && hbg::wordfinder_smem_bytes(threads, h.smem_diag_len) > (size_t)optin)
-        threads = ((threads / 2) + 31) / 32 * 32;
-    if (hbg::wordfinder_smem_bytes(threads, h.smem_diag_len) > (size_t)optin)
-        return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
     CU(hbg::wordfinder_configure());
-    int blocks_mode[2];
-    for (int mode = 0; mode < 2; ++mode) {
-        blocks_mode[mode] = o.num_blocksx;
-        if (blocks_mode[mode] <= 0) {
-            int sms = 1, per = 1;
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device);
-            if (hbg::wordfinder_occupancy(mode, threads, h.smem_diag_len, &per) != cudaSuccess || per < 1)
-                per = 1;
-            blocks_mode[mode] = sms * per;
-        }
-    }
+    std::vector<LaunchShape> shapes;   // host-side only; no device allocation
+    rc = plan_launches(batch, o, db->device, &shapes);
+    if (rc != HBG_OK)
+        return rc;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *base = (unsigned char *)scratch;
     unsigned int *tile = (unsigned int *)base;
@@ -1185,13 +1211,13 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     a.gdiag_len = 0;
     a.smem_diag = h.smem_diag_len;
     if (db->n > 0) {
-        for (int mode = 0; mode < 2; ++mode) {
-            if (batch->n_mode[mode] == 0)
-                continue;
-            a.group_list = batch->d_group_list + (mode ? batch->n_mode[0] : 0);
-            a.n_tiles = (int64_t)a.tiles_per_group * batch->n_mode[mode];
-            a.tile_counter = tile + mode;
-            CU(hbg::launch_wordfinder(a, mode, blocks_mode[mode], threads, st));
+        for (size_t c = 0; c < batch->classes.size(); ++c) {
+            const LaunchClass &lc = batch->classes[c];
+            a.group_list = batch->d_group_list + lc.first;
+            a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
+            a.tile_counter = tile + c;
+            a.smem_diag = lc.smem_diag;
+            CU(hbg::launch_wordfinder(a, lc.mode, shapes[c].blocks, shapes[c].threads, st));
         }
     }
     // per-query extension and kept counts follow the HSP count in d_counts
