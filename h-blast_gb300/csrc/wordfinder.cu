@@ -52,37 +52,87 @@ struct __align__(16) Smem {   // 16-byte size: the per-warp tables after it are 
 
 __device__ __forceinline__ int sc(const int8_t *m, int q, int s) { return m[q * 32 + s]; }
 
-// X-drop walk to the left from (s_off, q_off) inclusive; returns the best
-// score, *len = letters in the best walk.
+// Four letters from p (any alignment): two aligned 32-bit loads and a funnel
+// shift.  Reads up to 7 bytes past p; the database and batch letter buffers
+// carry 64 bytes of tail padding, and walks only take blocks that start at or
+// after the sequence start.
+__device__ __forceinline__ uint32_t load4(const uint8_t *p) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    return __funnelshift_r(__ldg(w), __ldg(w + 1), (uint32_t)(a & 3) * 8);
+}
+
+// X-drop walk to the left from (s_off, q_off) inclusive, at most
+// min(s_off, q_off) + 1 letters; returns the best score, *len = letters in
+// the best walk.  Letters are read four at a time; every letter is checked.
 __device__ int extend_left(const int8_t *m, const uint8_t *s, const uint8_t *q, int s_off,
                            int q_off, int dropoff, int *len) {
-    int n = min(s_off, q_off);
+    const int n = min(s_off, q_off);
     int best_i = n + 1;
     int score = 0, maxscore = 0;
-    const uint8_t *sp = s + s_off - n;
-    const uint8_t *qp = q + q_off - n;
-    for (int i = n; i >= 0; --i) {
-        score += sc(m, qp[i], sp[i]);
+    int k = 0;             // letters taken: the next is (s_off - k, q_off - k), index i = n - k
+    bool stop = false;
+    while (!stop && k + 3 <= n) {
+        const uint32_t sw = load4(s + s_off - k - 3);
+        const uint32_t qw = load4(q + q_off - k - 3);
+#pragma unroll
+        for (int j = 3; j >= 0; --j) {
+            score += sc(m, (qw >> (8 * j)) & 255u, (sw >> (8 * j)) & 255u);
+            if (score > maxscore) {
+                maxscore = score;
+                best_i = n - k - (3 - j);
+            }
+            if (maxscore - score >= dropoff) {
+                stop = true;
+                break;
+            }
+        }
+        k += 4;
+    }
+    for (; !stop && k <= n; ++k) {
+        score += sc(m, q[q_off - k], s[s_off - k]);
         if (score > maxscore) {
             maxscore = score;
-            best_i = i;
+            best_i = n - k;
         }
         if (maxscore - score >= dropoff)
-            break;
+            stop = true;
     }
     *len = n - best_i + 1;
     return maxscore;
 }
 
-// X-drop walk to the right that also stops when the running score is <= 0.
+// X-drop walk to the right from (s_off, q_off) that also stops when the
+// running score is <= 0; *s_last_off = the last subject offset examined
+// (s_off + n when the walk reaches a sequence end).
 __device__ int extend_right(const int8_t *m, const uint8_t *s, int s_len, const uint8_t *q,
                             int q_len, int s_off, int q_off, int dropoff, int maxscore,
                             int *len, int *s_last_off) {
-    int n = min(s_len - s_off, q_len - q_off);
+    const int n = min(s_len - s_off, q_len - q_off);
     int best_i = -1;
     int score = maxscore;
-    int i;
-    for (i = 0; i < n; ++i) {
+    int i = 0;
+    bool stop = false;
+    while (!stop && i + 3 < n) {
+        const uint32_t sw = load4(s + s_off + i);
+        const uint32_t qw = load4(q + q_off + i);
+        int j = 0;
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            j = jj;
+            score += sc(m, (qw >> (8 * jj)) & 255u, (sw >> (8 * jj)) & 255u);
+            if (score > maxscore) {
+                maxscore = score;
+                best_i = i + jj;
+            }
+            if (score <= 0 || maxscore - score >= dropoff) {
+                stop = true;
+                break;
+            }
+        }
+        i += stop ? j : 4;
+    }
+    for (; !stop && i < n; ++i) {
         score += sc(m, q[q_off + i], s[s_off + i]);
         if (score > maxscore) {
             maxscore = score;
