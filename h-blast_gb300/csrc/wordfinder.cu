@@ -75,17 +75,15 @@ __device__ int extend_left(const int8_t *m, const uint8_t *s, const uint8_t *q, 
     while (!stop && k + 3 <= n) {
         const uint32_t sw = load4(s + s_off - k - 3);
         const uint32_t qw = load4(q + q_off - k - 3);
+        // four letters without branches: letters after a stop change nothing
 #pragma unroll
         for (int j = 3; j >= 0; --j) {
-            score += sc(m, (qw >> (8 * j)) & 255u, (sw >> (8 * j)) & 255u);
-            if (score > maxscore) {
-                maxscore = score;
-                best_i = n - k - (3 - j);
-            }
-            if (maxscore - score >= dropoff) {
-                stop = true;
-                break;
-            }
+            const int ns = score + sc(m, (qw >> (8 * j)) & 255u, (sw >> (8 * j)) & 255u);
+            const bool better = !stop && ns > maxscore;
+            best_i = better ? n - k - (3 - j) : best_i;
+            maxscore = better ? ns : maxscore;
+            stop = stop || maxscore - ns >= dropoff;
+            score = ns;
         }
         k += 4;
     }
@@ -116,21 +114,19 @@ __device__ int extend_right(const int8_t *m, const uint8_t *s, int s_len, const 
     while (!stop && i + 3 < n) {
         const uint32_t sw = load4(s + s_off + i);
         const uint32_t qw = load4(q + q_off + i);
-        int j = 0;
+        int adv = 4;           // letters before the stopping one
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-            j = jj;
-            score += sc(m, (qw >> (8 * jj)) & 255u, (sw >> (8 * jj)) & 255u);
-            if (score > maxscore) {
-                maxscore = score;
-                best_i = i + jj;
-            }
-            if (score <= 0 || maxscore - score >= dropoff) {
-                stop = true;
-                break;
-            }
+            const int ns = score + sc(m, (qw >> (8 * jj)) & 255u, (sw >> (8 * jj)) & 255u);
+            const bool better = !stop && ns > maxscore;
+            best_i = better ? i + jj : best_i;
+            maxscore = better ? ns : maxscore;
+            const bool end = !stop && (ns <= 0 || maxscore - ns >= dropoff);
+            adv = end ? jj : adv;
+            stop = stop || end;
+            score = stop ? score : ns;
         }
-        i += stop ? j : 4;
+        i += adv;
     }
     for (; !stop && i < n; ++i) {
         score += sc(m, q[q_off + i], s[s_off + i]);
@@ -247,43 +243,51 @@ struct Item {
     int first_query;
 };
 
+// One hit on a diagonal whose cell holds `state` (NCBI's two-hit rule, with
+// the pending marker): returns the new cell value; when `on`, sets want_task
+// (and left, the first hit's end) if the hit starts an extension and
+// want_blk if it has to wait behind one.  Branch-free, so that a warp whose
+// lanes take different cases runs it once.
+template <typename Cell>
+__device__ __forceinline__ uint32_t two_hit_step(uint32_t state, int s_h, int dofs, int window,
+                                                 uint32_t pend, bool on, bool &want_task,
+                                                 bool &want_blk, int &left) {
+    using T = CellTraits<Cell>;
+    const bool is_pend = state == pend;                  // an extension of this diagonal is queued
+    const bool flag = (state & T::kFlag) != 0;           // state = end of the last extension
+    const int32_t last = (int32_t)state - dofs;          // else: subject offset of the last hit
+    const int32_t diff = s_h - last;
+    const bool reset = flag ? (!is_pend && s_h + dofs >= (int32_t)(state & T::kLast)) : diff >= window;
+    const bool trig = !flag && diff < window && diff >= 3;
+    want_blk = want_blk || (on && is_pend);
+    want_task = want_task || (on && trig);
+    left = (on && trig) ? last + 3 : left;
+    return reset ? (uint32_t)(Cell)(s_h + dofs) : (trig ? pend : state);
+}
+
 // Apply one batch of hits (one per active lane, in CPU order by lane) to the
-// diagonal table.  Lanes sharing a diagonal go in lane order.  Warp-collective.
+// diagonal table.  Lanes sharing a diagonal go in lane order (rank = lanes of
+// the same diagonal below this one).  Warp-collective.
 template <typename Cell>
 __device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d, int s_h, int q,
                                            WarpQueue &wq, int &n_tasks, int &n_blk, int blk_out) {
     using T = CellTraits<Cell>;
     const unsigned am = __ballot_sync(0xffffffffu, act);
-    int rank = 0, maxrank = 0;
-    if (act) {
-        const unsigned grp = __match_any_sync(am, d);
-        rank = __popc(grp & lanemask_lt());
-        maxrank = __popc(grp) - 1;
-    }
-    maxrank = __reduce_max_sync(0xffffffffu, (unsigned)maxrank);
+    int rank = 0;
+    if (act)
+        rank = __popc(__match_any_sync(am, d) & lanemask_lt());
     const uint32_t pend = T::kFlag | (uint32_t)(it.dofs - 1);
     bool want_task = false, want_blk = false;
     int left = 0;
-    for (int rr = 0; rr <= maxrank; ++rr) {
-        if (act && rank == rr) {
-            const uint32_t cell = it.diag[d];
-            if (cell == pend) {
-                want_blk = true;
-            } else if (cell & T::kFlag) {
-                if (s_h + it.dofs >= (int32_t)(cell & T::kLast))
-                    it.diag[d] = (Cell)(s_h + it.dofs);
-            } else {
-                const int32_t last = (int32_t)cell - it.dofs;   // subject offset of the last hit
-                const int32_t diff = s_h - last;
-                if (diff >= it.window) {
-                    it.diag[d] = (Cell)(s_h + it.dofs);
-                } else if (diff >= 3) {
-                    want_task = true;
-                    left = last + 3;
-                    it.diag[d] = (Cell)pend;
-                }
-            }
-        }
+    for (int rr = 0; __any_sync(0xffffffffu, act && rank >= rr); ++rr) {
+        const bool mine = act && rank == rr;
+        uint32_t cell = 0;
+        if (mine)
+            cell = it.diag[d];
+        const uint32_t next = two_hit_step<Cell>(cell, s_h, it.dofs, it.window, pend, mine, want_task,
+                                                 want_blk, left);
+        if (mine && next != cell)
+            it.diag[d] = (Cell)next;
         __syncwarp();
     }
     // queue appends: tasks in any order; blocked hits in lane order, which
@@ -306,18 +310,23 @@ __device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d
     __syncwarp();
 }
 
-// One round: run every queued extension (lane per extension), then replay the
-// blocked hits once, in order.  Replayed hits may queue new extensions and be
-// blocked again behind them; that is safe mid-subject because every later hit
-// on a pending diagonal is blocked after them.  With drain, repeat until both
-// lists are empty (needed before the subject ends).  Warp-collective.
+// One round: run queued extensions (lane per extension; the newest 32 when at
+// least 32 wait, else all), then replay the blocked hits once, in order.
+// Extensions of distinct diagonals are independent, and a diagonal has at
+// most one queued extension, so any subset may run first.  Replayed hits may
+// queue new extensions and be blocked again behind them; that is safe
+// mid-subject because every later hit on a pending diagonal is blocked after
+// them.  Queues hold 64: a replay batch starts only while at most 32 tasks
+// wait.  With drain, run everything and repeat until both lists are empty
+// (needed before the subject ends).  Warp-collective.
 template <typename Cell>
 __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
                       int &n_tasks, int &n_blk, int &blk_cur, bool drain) {
     using T = CellTraits<Cell>;
     const int lane = threadIdx.x & 31;
     do {
-        for (int t0 = 0; t0 < n_tasks; t0 += 32) {
+        const int first = (!drain && n_tasks >= 32) ? n_tasks - 32 : 0;
+        for (int t0 = first; t0 < n_tasks; t0 += 32) {
             const int i = t0 + lane;
             if (i < n_tasks) {
                 const int s_h = wq.task_s[i], q = wq.task_q[i];
@@ -351,12 +360,23 @@ __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, W
             }
         }
         __syncwarp();
-        n_tasks = 0;
+        n_tasks = first;
         const int nb = n_blk;
         const int src = blk_cur;
         n_blk = 0;
         blk_cur ^= 1;
         for (int b0 = 0; b0 < nb; b0 += 32) {
+            if (n_tasks > 32) {
+                // no room for the tasks another batch may queue: the rest of
+                // the list follows the re-blocked hits, in order
+                for (int i = b0 + lane; i < nb; i += 32) {
+                    wq.blk_s[blk_cur][n_blk + i - b0] = wq.blk_s[src][i];
+                    wq.blk_q[blk_cur][n_blk + i - b0] = wq.blk_q[src][i];
+                }
+                n_blk += nb - b0;
+                __syncwarp();
+                break;
+            }
             const int i = b0 + lane;
             const bool act = i < nb;
             int s_h = 0, q = 0, d = 0;
@@ -509,22 +529,10 @@ __device__ __forceinline__ void apply_offset(const Item<Cell> &it, bool act, int
     if (act) {
         const int d = (q - s_h) & it.mask;
         const uint32_t cell = it.diag[d];
-        if (cell == pend) {
-            want_blk = true;
-        } else if (cell & T::kFlag) {
-            if (s_h + it.dofs >= (int32_t)(cell & T::kLast))
-                it.diag[d] = (Cell)(s_h + it.dofs);
-        } else {
-            const int32_t last = (int32_t)cell - it.dofs;
-            const int32_t diff = s_h - last;
-            if (diff >= it.window) {
-                it.diag[d] = (Cell)(s_h + it.dofs);
-            } else if (diff >= 3) {
-                want_task = true;
-                left = last + 3;
-                it.diag[d] = (Cell)pend;
-            }
-        }
+        const uint32_t next = two_hit_step<Cell>(cell, s_h, it.dofs, it.window, pend, true, want_task,
+                                                 want_blk, left);
+        if (next != cell)
+            it.diag[d] = (Cell)next;
     }
     if (__any_sync(0xffffffffu, want_task || want_blk)) {
         const unsigned tm = __ballot_sync(0xffffffffu, want_task);
