@@ -266,30 +266,48 @@ __device__ __forceinline__ uint32_t two_hit_step(uint32_t state, int s_h, int do
 }
 
 // Apply one batch of hits (one per active lane, in CPU order by lane) to the
-// diagonal table.  Lanes sharing a diagonal go in lane order (rank = lanes of
-// the same diagonal below this one).  Warp-collective.
+// diagonal table.  Lanes sharing a diagonal form a chain in lane order (rank =
+// lanes of the same diagonal below this one); a chain's state moves from lane
+// to lane by shuffles, so the table is read and written once per diagonal.
+// Warp-collective.
 template <typename Cell>
 __device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d, int s_h, int q,
                                            WarpQueue &wq, int &n_tasks, int &n_blk, int blk_out) {
     using T = CellTraits<Cell>;
+    const int lane = threadIdx.x & 31;
     const unsigned am = __ballot_sync(0xffffffffu, act);
-    int rank = 0;
-    if (act)
-        rank = __popc(__match_any_sync(am, d) & lanemask_lt());
+    unsigned grp = 0;
+    int rank = 0, prev = lane, head = lane;
+    if (act) {
+        grp = __match_any_sync(am, d);
+        const unsigned below = grp & lanemask_lt();
+        rank = __popc(below);
+        if (below)
+            prev = 31 - __clz(below);
+        head = __ffs(grp) - 1;
+    }
+    const bool tail = act && (grp >> lane) == 1u;       // last lane of its chain
     const uint32_t pend = T::kFlag | (uint32_t)(it.dofs - 1);
     bool want_task = false, want_blk = false;
     int left = 0;
-    for (int rr = 0; __any_sync(0xffffffffu, act && rank >= rr); ++rr) {
+    uint32_t orig = 0;
+    if (act && rank == 0)
+        orig = it.diag[d];
+    uint32_t state = two_hit_step<Cell>(orig, s_h, it.dofs, it.window, pend, act && rank == 0,
+                                        want_task, want_blk, left);
+    bool chained = false;
+    for (int rr = 1; __any_sync(0xffffffffu, act && rank >= rr); ++rr) {
+        const uint32_t ps = __shfl_sync(0xffffffffu, state, prev);
         const bool mine = act && rank == rr;
-        uint32_t cell = 0;
-        if (mine)
-            cell = it.diag[d];
-        const uint32_t next = two_hit_step<Cell>(cell, s_h, it.dofs, it.window, pend, mine, want_task,
-                                                 want_blk, left);
-        if (mine && next != cell)
-            it.diag[d] = (Cell)next;
-        __syncwarp();
+        const uint32_t nx = two_hit_step<Cell>(ps, s_h, it.dofs, it.window, pend, mine, want_task,
+                                               want_blk, left);
+        state = mine ? nx : state;
+        chained = true;
     }
+    if (chained)
+        orig = __shfl_sync(0xffffffffu, orig, head);
+    if (tail && state != orig)
+        it.diag[d] = (Cell)state;
     // queue appends: tasks in any order; blocked hits in lane order, which
     // keeps hits of one diagonal in CPU order
     const unsigned tm = __ballot_sync(0xffffffffu, want_task);
