@@ -48,7 +48,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="hblast", choices=["hblast", "reference"])
-    p.add_argument("--config", default="batched", choices=["batched", "plain", "blastx", "served", "autotune"])
+    p.add_argument("--config", default="batched", choices=["batched", "plain", "blastx", "served", "autotune", "ingest"])
     p.add_argument("--rates", default="2,5,10,20", help="served: Poisson arrival rates (queries/s)")
     p.add_argument("--requests", type=int, default=60, help="served: requests per rate")
     p.add_argument("--subjects", type=int, default=0, help="override the database size (testing)")
@@ -221,7 +221,14 @@ def served_arm(args):
     out = {"metric": "served latency", "config": {"workload": f"served mixed stream vs {n_sub} subjects "
                                                                f"({ssum} residues)", "requests_per_rate": args.requests}}
     rates = [float(x) for x in args.rates.split(",")]
-    for form in ("served", "plain"):
+    forms = {"served": dict(max_inflight=2, max_batch_queries=512),
+             "served_fifo": dict(max_inflight=2, max_batch_queries=512, max_batch_letters=0, shortest_first_ms=0),
+             "plain": dict(max_inflight=1, max_batch_queries=1, max_batch_letters=0, shortest_first_ms=0)}
+    out["forms"] = {"served": "library defaults: shortest-first admission (age bound 2 s), <= 8192 query "
+                              "letters per batch, 2 batches in flight",
+                    "served_fifo": "arrival-order admission, no letter cap, 2 batches in flight",
+                    "plain": "one query per launch, one at a time, arrival order"}
+    for form, so in forms.items():
         res_form = []
         for rate in rates:
             r = np.random.default_rng(int(rate * 1000) + 7)
@@ -234,8 +241,6 @@ def served_arm(args):
                 else:
                     reqs.append(("x", r.integers(0, 4, size=int(r.integers(300, 3001))).astype(np.uint8)))
             gaps = r.exponential(1.0 / rate, size=args.requests)
-            so = dict(max_inflight=2, max_batch_queries=512) if form == "served" else \
-                dict(max_inflight=1, max_batch_queries=1)
             srv = hblast.Server(gdb, **so)
             tickets = []
             letters = 0
@@ -304,6 +309,59 @@ def autotune_arm(args):
     print(json.dumps(report), flush=True)
 
 
+def ingest_arm(args):
+    """Opening the batched workload's database from NCBI BLAST files (three format-4 volumes under
+    an alias, in the page cache) into device memory, against opening it from host arrays and
+    against reading the files into host arrays only."""
+    import shutil
+    import tempfile
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as g
+    g.build()
+    import hblast
+    from hblast import blastdb, synth
+    _, db = synth.batched_blastp(seed=0, n_queries=1, n_subjects=args.subjects or 2_000_000)
+    tmp = tempfile.mkdtemp(prefix="hbg_ingest_")
+    try:
+        names = blastdb.write(os.path.join(tmp, "db"), db.residues, db.offsets, volume_residues=256 << 20)
+        path = os.path.join(tmp, "db")
+        psq_bytes = sum(os.path.getsize(os.path.join(tmp, n + ".psq")) for n in names)
+
+        def timed(fn):
+            for _ in range(args.warmup):
+                fn()
+            ts = []
+            for _ in range(args.steps):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t)
+            return float(np.median(ts))
+
+        t_files = timed(lambda: hblast.Database.from_blastdb(path).close())
+        t_arrays = timed(lambda: hblast.Database(db.residues, db.offsets).close())
+        t_host = timed(lambda: hblast.blastdb_read(path))
+        # the two resident databases search alike
+        a, b = hblast.Database(db.residues, db.offsets), hblast.Database.from_blastdb(path)
+        same = a.info()[:2] == b.info()[:2]
+        a.close(), b.close()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    gbs = psq_bytes / t_files / 1e9
+    print(json.dumps({
+        "metric": "database ingest GB/s", "value": gbs, "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_files * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded; BLOSUM62-implied background)",
+        "config": {"workload": f"hbg_db_open_blastdb of {len(names)} format-4 volumes ({psq_bytes} .psq bytes, "
+                               f"{db.n} subjects) from the page cache, open + close per step",
+                   "same_counts_as_arrays": same},
+        "from_arrays_ms": t_arrays * 1e3, "from_arrays_gbs": psq_bytes / t_arrays / 1e9,
+        "host_read_only_ms": t_host * 1e3, "host_read_only_gbs": psq_bytes / t_host / 1e9,
+    }), flush=True)
+
+
 # --------------------------------------------------------------------------- GPU arm
 
 def main():
@@ -317,6 +375,9 @@ def main():
         return
     if args.config == "autotune":
         autotune_arm(args)
+        return
+    if args.config == "ingest":
+        ingest_arm(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

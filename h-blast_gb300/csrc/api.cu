@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../host/batch_builder.h"
+#include "../host/blastdb.h"
 #include "kernels.h"
 
 namespace {
@@ -517,44 +518,32 @@ int hbg_default_gpu_options(hbg_gpu_options *opt) {
     return HBG_OK;
 }
 
-int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n,
-                const hbg_gpu_options *opt, hbg_db **out) {
-    if (!out || !offsets || n < 0 || (n > 0 && !residues))
-        return fail(HBG_ERR_INVALID, "hbg_db_open: null argument or negative count");
-    *out = nullptr;
-    hbg_gpu_options o;
-    hbg_default_gpu_options(&o);
+}  // extern "C"
+
+namespace {
+
+// Checks shared by the database entry points: options, device.
+int db_device(const hbg_gpu_options *opt, hbg_gpu_options *o) {
+    hbg_default_gpu_options(o);
     if (opt)
-        o = *opt;
-    if (!o.use_gpu)
+        *o = *opt;
+    if (!o->use_gpu)
         return fail(HBG_ERR_NO_DEVICE, "use_gpu is 0 and this library has no CPU path");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(HBG_ERR_NO_DEVICE, "no CUDA device");
-    if (o.method < 0 || o.method >= ndev)
+    if (o->method < 0 || o->method >= ndev)
         return fail(HBG_ERR_INVALID, "method selects a device that does not exist");
-    // validate and lay out: one sentinel before every subject and after the last
-    std::vector<int64_t> off(n);
-    std::vector<int32_t> len(n);
-    int64_t pos = 1, total = 0;
-    int32_t max_len = 0;
-    for (int32_t i = 0; i < n; ++i) {
-        int64_t L = offsets[i + 1] - offsets[i];
-        if (L < 0 || L > HBG_MAX_SUBJECT_LEN)
-            return fail(L < 0 ? HBG_ERR_INVALID : HBG_ERR_TOO_LONG,
-                        "subject " + std::to_string(i) + ": bad length");
-        const uint8_t *s = residues + offsets[i];
-        for (int64_t k = 0; k < L; ++k)
-            if (s[k] == 0 || s[k] >= HBG_ALPHABET)
-                return fail(HBG_ERR_INVALID, "subject " + std::to_string(i) +
-                                                 ": letter outside NCBIstdaa 1..27");
-        off[i] = pos;
-        len[i] = (int32_t)L;
-        pos += L + 1;
-        total += L;
-        max_len = std::max<int32_t>(max_len, (int32_t)L);
-    }
-    const int64_t letters_len = pos + 64;
+    return HBG_OK;
+}
+
+// Allocate the resident database for a validated layout (subject i at
+// device offset off[i], len[i] letters, sentinels between), let `fill` copy
+// the letters (it returns "" or an error), then the offsets, the
+// length-descending schedule and the word histogram.
+template <typename Fill>
+int db_create(int device, int32_t n, const std::vector<int64_t> &off, const std::vector<int32_t> &len,
+              int64_t total, int32_t max_len, int64_t letters_len, Fill &&fill, hbg_db **out) {
     std::vector<int32_t> order(n);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
@@ -563,7 +552,7 @@ int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n,
     hbg_db *db = new (std::nothrow) hbg_db;
     if (!db)
         return fail(HBG_ERR_NOMEM, "host allocation");
-    db->device = o.method;
+    db->device = device;
     DeviceScope ds(db->device);
     auto bail = [&](int code) {
         dfree(db->d_letters);
@@ -587,22 +576,11 @@ int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n,
     CUB(dalloc(&db->d_order, (size_t)n));
     CUB(dalloc(&db->d_hist, HBG_NUM_CELLS));
     CUB(cudaMemset(db->d_letters, 0, (size_t)letters_len));
-    // copy subjects with their sentinels through a staging buffer of ~64 MiB
     {
-        int32_t i = 0;
-        std::vector<uint8_t> stage;
-        while (i < n) {
-            const int64_t start_dev = off[i] - 1;
-            stage.clear();
-            stage.push_back(0);
-            while (i < n && (int64_t)stage.size() < (64 << 20)) {
-                const uint8_t *s = residues + offsets[i];
-                stage.insert(stage.end(), s, s + len[i]);
-                stage.push_back(0);
-                ++i;
-            }
-            CUB(cudaMemcpy(db->d_letters + start_dev, stage.data(), stage.size(), cudaMemcpyHostToDevice));
-        }
+        int code = HBG_OK;
+        std::string err = fill(db->d_letters, &code);
+        if (!err.empty())
+            return bail(fail(code, err));
     }
     if (n > 0) {
         CUB(cudaMemcpy(db->d_off, off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
@@ -620,6 +598,253 @@ int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n,
     db->bytes = letters_len + (int64_t)n * 16 + HBG_NUM_CELLS * 8;
     *out = db;
     return HBG_OK;
+}
+
+std::string cuda_msg(const char *what, cudaError_t e, int *code) {
+    *code = e == cudaErrorMemoryAllocation ? HBG_ERR_NOMEM : HBG_ERR_CUDA;
+    return std::string(what) + ": " + cudaGetErrorString(e);
+}
+
+// Volumes of a BLAST database with their place in the resident layout:
+// volume v's .psq byte b lands at device offset base[v] + b (a volume's
+// leading 0 is the previous volume's last separator).
+struct BlastDbPlan {
+    std::vector<hbg::BlastDbVolume> vols;
+    std::vector<int64_t> base;
+    int64_t n = 0, total = 0, bytes = 0;
+    int32_t max_len = 0;
+};
+
+int blastdb_plan(const char *path, BlastDbPlan *plan) {
+    if (!path)
+        return fail(HBG_ERR_INVALID, "null database name");
+    std::vector<std::string> names;
+    std::string err = hbg::blastdb_volumes(path, &names);
+    if (!err.empty())
+        return fail(HBG_ERR_INVALID, err);
+    plan->vols.resize(names.size());
+    int64_t at = 0;
+    for (size_t v = 0; v < names.size(); ++v) {
+        err = hbg::blastdb_read_index(names[v], &plan->vols[v]);
+        if (!err.empty())
+            return fail(HBG_ERR_INVALID, err);
+        const hbg::BlastDbVolume &V = plan->vols[v];
+        if (V.max_len > HBG_MAX_SUBJECT_LEN)
+            return fail(HBG_ERR_TOO_LONG, names[v] + ": a sequence longer than the subject limit");
+        plan->base.push_back(v == 0 ? 0 : at - 1);
+        at = plan->base.back() + V.psq_bytes;
+        plan->n += V.n;
+        plan->total += V.residues;
+        plan->max_len = std::max(plan->max_len, V.max_len);
+    }
+    if (plan->n > 0x7fffffff)
+        return fail(HBG_ERR_TOO_LONG, "more than 2^31 - 1 sequences");
+    plan->bytes = at;
+    return HBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hbg_db_open(const uint8_t *residues, const int64_t *offsets, int32_t n,
+                const hbg_gpu_options *opt, hbg_db **out) {
+    if (!out || !offsets || n < 0 || (n > 0 && !residues))
+        return fail(HBG_ERR_INVALID, "hbg_db_open: null argument or negative count");
+    *out = nullptr;
+    hbg_gpu_options o;
+    int rc = db_device(opt, &o);
+    if (rc != HBG_OK)
+        return rc;
+    // validate and lay out: one sentinel before every subject and after the last
+    std::vector<int64_t> off(n);
+    std::vector<int32_t> len(n);
+    int64_t pos = 1, total = 0;
+    int32_t max_len = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        int64_t L = offsets[i + 1] - offsets[i];
+        if (L < 0 || L > HBG_MAX_SUBJECT_LEN)
+            return fail(L < 0 ? HBG_ERR_INVALID : HBG_ERR_TOO_LONG,
+                        "subject " + std::to_string(i) + ": bad length");
+        const uint8_t *s = residues + offsets[i];
+        for (int64_t k = 0; k < L; ++k)
+            if (s[k] == 0 || s[k] >= HBG_ALPHABET)
+                return fail(HBG_ERR_INVALID, "subject " + std::to_string(i) +
+                                                 ": letter outside NCBIstdaa 1..27");
+        off[i] = pos;
+        len[i] = (int32_t)L;
+        pos += L + 1;
+        total += L;
+        max_len = std::max<int32_t>(max_len, (int32_t)L);
+    }
+    const int64_t letters_len = pos + 64;
+    // copy subjects with their sentinels through a staging buffer of ~64 MiB
+    auto fill = [&](uint8_t *d_letters, int *code) -> std::string {
+        int32_t i = 0;
+        std::vector<uint8_t> stage;
+        while (i < n) {
+            const int64_t start_dev = off[i] - 1;
+            stage.clear();
+            stage.push_back(0);
+            while (i < n && (int64_t)stage.size() < (64 << 20)) {
+                const uint8_t *s = residues + offsets[i];
+                stage.insert(stage.end(), s, s + len[i]);
+                stage.push_back(0);
+                ++i;
+            }
+            cudaError_t e = cudaMemcpy(d_letters + start_dev, stage.data(), stage.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess)
+                return cuda_msg("cudaMemcpy (subjects)", e, code);
+        }
+        return std::string();
+    };
+    return db_create(o.method, n, off, len, total, max_len, letters_len, fill, out);
+}
+
+int hbg_blastdb_info(const char *path, int32_t *n_subjects, int64_t *n_residues, int32_t *max_len,
+                     int32_t *n_volumes) {
+    BlastDbPlan plan;
+    int rc = blastdb_plan(path, &plan);
+    if (rc != HBG_OK)
+        return rc;
+    if (n_subjects)
+        *n_subjects = (int32_t)plan.n;
+    if (n_residues)
+        *n_residues = plan.total;
+    if (max_len)
+        *max_len = plan.max_len;
+    if (n_volumes)
+        *n_volumes = (int32_t)plan.vols.size();
+    return HBG_OK;
+}
+
+int hbg_blastdb_read(const char *path, uint8_t *residues, int64_t *offsets) {
+    if (!offsets)
+        return fail(HBG_ERR_INVALID, "hbg_blastdb_read: null offsets");
+    BlastDbPlan plan;
+    int rc = blastdb_plan(path, &plan);
+    if (rc != HBG_OK)
+        return rc;
+    if (plan.total > 0 && !residues)
+        return fail(HBG_ERR_INVALID, "hbg_blastdb_read: null residues");
+    std::vector<uint8_t> buf;
+    int64_t at = 0, k = 0;
+    offsets[0] = 0;
+    for (const hbg::BlastDbVolume &V : plan.vols) {
+        buf.resize((size_t)V.psq_bytes);
+        std::string err = hbg::blastdb_read_psq(V, 0, V.psq_bytes, buf.data());
+        if (!err.empty())
+            return fail(HBG_ERR_INVALID, err);
+        for (int32_t i = 0; i < V.n; ++i) {
+            const int64_t L = (int64_t)V.seq_off[i + 1] - V.seq_off[i] - 1;
+            memcpy(residues + at, buf.data() + V.seq_off[i], (size_t)L);
+            at += L;
+            offsets[++k] = at;
+        }
+    }
+    return HBG_OK;
+}
+
+int hbg_db_open_blastdb(const char *path, const hbg_gpu_options *opt, hbg_db **out) {
+    if (!out)
+        return fail(HBG_ERR_INVALID, "hbg_db_open_blastdb: null out");
+    *out = nullptr;
+    hbg_gpu_options o;
+    int rc = db_device(opt, &o);
+    if (rc != HBG_OK)
+        return rc;
+    BlastDbPlan plan;
+    rc = blastdb_plan(path, &plan);
+    if (rc != HBG_OK)
+        return rc;
+    const int32_t n = (int32_t)plan.n;
+    std::vector<int64_t> off(n);
+    std::vector<int32_t> len(n);
+    {
+        int64_t k = 0;
+        for (size_t v = 0; v < plan.vols.size(); ++v) {
+            const hbg::BlastDbVolume &V = plan.vols[v];
+            for (int32_t i = 0; i < V.n; ++i, ++k) {
+                off[k] = plan.base[v] + V.seq_off[i];
+                len[k] = (int32_t)(V.seq_off[i + 1] - V.seq_off[i] - 1);
+            }
+        }
+    }
+    const int64_t letters_len = plan.bytes + 64;
+    // each volume's .psq is already the device layout: read whole sequences
+    // in ~64 MiB pieces into two pinned buffers, checking each piece while
+    // the previous one is copied
+    auto fill = [&](uint8_t *d_letters, int *code) -> std::string {
+        const size_t piece = std::max<size_t>(64u << 20, (size_t)plan.max_len + 2);
+        uint8_t *pin[2] = {nullptr, nullptr};
+        cudaStream_t st = nullptr;
+        cudaEvent_t done[2] = {nullptr, nullptr};
+        std::string err;
+        cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+            e = cudaMallocHost(&pin[j], piece);
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&done[j], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess)
+            err = cuda_msg("staging buffers", e, code);
+        int cur = 0;
+        bool used[2] = {false, false};
+        for (size_t v = 0; v < plan.vols.size() && err.empty(); ++v) {
+            const hbg::BlastDbVolume &V = plan.vols[v];
+            int32_t i = 0;
+            int64_t from = 0;                      // the leading 0 of volume 0 is copied too
+            while (err.empty() && (from == 0 || i < V.n)) {
+                // whole sequences (with separators) up to the piece size
+                int32_t j = i;
+                while (j < V.n && (int64_t)V.seq_off[j + 1] - from <= (int64_t)piece)
+                    ++j;
+                if (j == i && i < V.n)
+                    j = i + 1;                     // piece >= longest + 2, so one always fits
+                const int64_t to = i < V.n ? (int64_t)V.seq_off[j] : (int64_t)V.seq_off[0];
+                if (used[cur]) {
+                    e = cudaEventSynchronize(done[cur]);
+                    if (e != cudaSuccess) {
+                        err = cuda_msg("cudaEventSynchronize", e, code);
+                        break;
+                    }
+                }
+                err = hbg::blastdb_read_psq(V, from, to - from, pin[cur]);
+                if (!err.empty()) {
+                    *code = HBG_ERR_INVALID;
+                    break;
+                }
+                // volume v > 0: its leading 0 is already in place (the buffer starts zeroed)
+                const int64_t skip = (from == 0 && v > 0) ? 1 : 0;
+                e = cudaMemcpyAsync(d_letters + plan.base[v] + from + skip, pin[cur] + skip,
+                                    (size_t)(to - from - skip), cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess)
+                    e = cudaEventRecord(done[cur], st);
+                if (e != cudaSuccess) {
+                    err = cuda_msg("cudaMemcpyAsync (volume)", e, code);
+                    break;
+                }
+                used[cur] = true;
+                cur ^= 1;
+                from = to;
+                i = j;
+            }
+        }
+        if (st) {
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess && err.empty())
+                err = cuda_msg("cudaStreamSynchronize", e, code);
+            cudaStreamDestroy(st);
+        }
+        for (int j = 0; j < 2; ++j) {
+            if (done[j])
+                cudaEventDestroy(done[j]);
+            if (pin[j])
+                cudaFreeHost(pin[j]);
+        }
+        return err;
+    };
+    return db_create(o.method, n, off, len, plan.total, plan.max_len, letters_len, fill, out);
 }
 
 int hbg_db_close(hbg_db *db) {

@@ -56,9 +56,11 @@ class RuntimeOptions(C.Structure):
 
 
 class ServerOptions(C.Structure):
-    """hbg_server_options: slots in flight, queries per batch, memory budget, group length."""
+    """hbg_server_options: slots in flight, queries per batch, memory budget, group length, letters per
+    batch, shortest-first admission age."""
     _fields_ = [("max_inflight", C.c_int32), ("max_batch_queries", C.c_int32), ("memory_budget", C.c_int64),
-                ("max_group_len", C.c_int32), ("pad", C.c_int32)]
+                ("max_group_len", C.c_int32), ("max_batch_letters", C.c_int32), ("shortest_first_ms", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 class QueryStats(C.Structure):
@@ -75,6 +77,10 @@ _SIGS = {
     "hbg_read_runtime_options": ([C.c_char_p, C.POINTER(RuntimeOptions)], C.c_int),
     "hbg_db_open": ([_P, _P, C.c_int32, C.POINTER(GpuOptions), C.POINTER(_P)], C.c_int),
     "hbg_db_close": ([_P], C.c_int),
+    "hbg_blastdb_info": ([C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                          C.POINTER(C.c_int32)], C.c_int),
+    "hbg_blastdb_read": ([C.c_char_p, _P, _P], C.c_int),
+    "hbg_db_open_blastdb": ([C.c_char_p, C.POINTER(GpuOptions), C.POINTER(_P)], C.c_int),
     "hbg_db_info": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
     "hbg_batch_create": ([C.POINTER(_Query), C.c_int32, C.POINTER(_WordParams), C.c_int32, C.POINTER(_P)], C.c_int),
     "hbg_batch_create_blastx": ([C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_int32), C.c_int32,
@@ -182,8 +188,24 @@ class ProteinQuery:
         return int(self.context_offset[-1] + self.context_length[-1])
 
 
+def blastdb_info(path) -> dict:
+    """Counts of an NCBI BLAST protein database without reading its sequences."""
+    n, r, m, v = C.c_int32(), C.c_int64(), C.c_int32(), C.c_int32()
+    _check(lib().hbg_blastdb_info(str(path).encode(), C.byref(n), C.byref(r), C.byref(m), C.byref(v)))
+    return dict(n_subjects=n.value, n_residues=r.value, max_len=m.value, n_volumes=v.value)
+
+
+def blastdb_read(path):
+    """(residues, offsets) of an NCBI BLAST protein database, in Database's input form."""
+    info = blastdb_info(path)
+    res = np.zeros(max(info["n_residues"], 1), dtype=np.uint8)
+    off = np.zeros(info["n_subjects"] + 1, dtype=np.int64)
+    _check(lib().hbg_blastdb_read(str(path).encode(), res.ctypes.data, off.ctypes.data))
+    return res[:info["n_residues"]], off
+
+
 class Database:
-    """Subjects resident in device memory (hbg_db_open)."""
+    """Subjects resident in device memory (hbg_db_open, or hbg_db_open_blastdb via from_blastdb)."""
 
     def __init__(self, residues: np.ndarray, offsets: np.ndarray, options: GpuOptions | None = None):
         self.residues = np.ascontiguousarray(residues, dtype=np.uint8)
@@ -194,6 +216,18 @@ class Database:
                                  C.byref(options) if options is not None else None, C.byref(h)))
         self.handle = h
         self.n_subjects = n
+
+    @classmethod
+    def from_blastdb(cls, path, options: GpuOptions | None = None) -> "Database":
+        """Open an NCBI BLAST protein database (.pal or .pin/.psq) straight into device memory."""
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        _check(lib().hbg_db_open_blastdb(str(path).encode(), C.byref(options) if options is not None else None,
+                                         C.byref(h)))
+        self.handle = h
+        self.residues = self.offsets = None
+        self.n_subjects = self.info()[0]
+        return self
 
     def info(self):
         n, r, b = C.c_int32(), C.c_int64(), C.c_int64()

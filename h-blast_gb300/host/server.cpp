@@ -2,10 +2,16 @@
 //
 // A dispatcher thread owns max_inflight slots (a CUDA stream plus a reusable
 // search result each).  Whenever a slot is free and requests are waiting it
-// admits waiting requests in arrival order -- as many as fit the memory
-// budget (lookup tables + HSP buffers of everything in flight) and the batch
-// size cap -- builds their batch on the host and launches the search on the
-// slot's stream, so batches overlap with each other's host work and GPU tail.
+// admits waiting requests -- as many as fit the memory budget (lookup tables
+// + HSP buffers of everything in flight), the batch size cap and the cap on
+// query letters per batch -- builds their batch on the host and launches the
+// search on the slot's stream, so batches overlap with each other's host work
+// and GPU tail.  Admission order is arrival order, or (shortest_first_ms > 0)
+// requests that have waited that long first, then the shortest: with query
+// lengths spread over three decades, short requests stop queueing behind
+// long ones, and no request waits behind newer ones for longer than the age
+// bound.  A batch's results come back together, so the letter cap keeps one
+// batch from holding its short requests for the time of many long ones.
 // A finished slot's HSPs are split per request.  Queries in one batch are
 // searched independently (own diagonals, own bounds), so every request's
 // result equals a search of it alone.
@@ -16,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -212,19 +219,42 @@ void dispatcher(hbg_server *S) {
                 break;
             }
         if (free_slot && !S->pending.empty()) {
+            std::vector<int64_t> cand(S->pending.begin(), S->pending.end());
+            if (S->so.shortest_first_ms > 0) {
+                const Clock::time_point now = Clock::now();
+                const auto aged = [&](int64_t id) {
+                    return std::chrono::duration<double, std::milli>(now - S->reqs[id].t0).count() >=
+                           S->so.shortest_first_ms;
+                };
+                auto mid = std::stable_partition(cand.begin(), cand.end(), aged);
+                std::stable_sort(mid, cand.end(), [&](int64_t x, int64_t y) {
+                    return S->reqs[x].seq.size() < S->reqs[y].seq.size();
+                });
+            }
             std::vector<int64_t> ids;
-            int64_t bytes = 0;
-            while (!S->pending.empty() && (int32_t)ids.size() < S->so.max_batch_queries) {
-                const Request &r = S->reqs[S->pending.front()];
+            int64_t bytes = 0, letters = 0;
+            for (int64_t id : cand) {
+                if ((int32_t)ids.size() >= S->so.max_batch_queries)
+                    break;
+                const Request &r = S->reqs[id];
                 const int64_t room = S->so.memory_budget - S->inflight_bytes - bytes;
-                // admit while the budget holds; an oversized request runs alone
+                // admit while the budget and the letter cap hold; an oversized
+                // request runs alone
                 if (r.est_bytes > room && !(ids.empty() && S->inflight_bytes == 0))
                     break;
-                ids.push_back(S->pending.front());
+                if (S->so.max_batch_letters > 0 && !ids.empty() &&
+                    letters + (int64_t)r.seq.size() > S->so.max_batch_letters)
+                    break;
+                ids.push_back(id);
                 bytes += r.est_bytes;
-                S->pending.pop_front();
+                letters += (int64_t)r.seq.size();
             }
             if (!ids.empty()) {
+                std::deque<int64_t> rest;
+                for (int64_t id : S->pending)
+                    if (std::find(ids.begin(), ids.end(), id) == ids.end())
+                        rest.push_back(id);
+                S->pending.swap(rest);
                 launch_slot(S, *free_slot, ids, bytes, lk);
                 continue;
             }
@@ -247,6 +277,8 @@ int hbg_server_default_options(hbg_server_options *o) {
     o->max_batch_queries = 512;
     o->memory_budget = (int64_t)32 << 30;
     o->max_group_len = 0;
+    o->max_batch_letters = 8192;
+    o->shortest_first_ms = 2000;
     o->pad = 0;
     return HBG_OK;
 }
@@ -266,7 +298,7 @@ int hbg_server_create(hbg_db *db, const hbg_word_params *params, const hbg_gpu_o
     if (sopt)
         S->so = *sopt;
     if (S->so.max_inflight < 1 || S->so.max_inflight > 16 || S->so.max_batch_queries < 1 ||
-        S->so.memory_budget <= 0) {
+        S->so.memory_budget <= 0 || S->so.max_batch_letters < 0 || S->so.shortest_first_ms < 0) {
         delete S;
         return HBG_ERR_INVALID;
     }

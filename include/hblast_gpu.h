@@ -160,6 +160,37 @@ int hbg_db_close(hbg_db *db);
 int hbg_db_info(const hbg_db *db, int32_t *n_subjects, int64_t *n_residues,
                 int64_t *device_bytes);
 
+/* ---- NCBI BLAST databases on disk ------------------------------------------ */
+
+/* `path` names a protein BLAST database as blastp's -db does: `path`.pal (an
+ * alias whose DBLIST names the volumes, relative to the alias file) or a
+ * single volume `path`.pin + `path`.psq, NCBI format version 4 (what
+ * makeblastdb 2.2.28 writes).  H-BLAST reads the same files only to count
+ * each volume's sequences (ExtractVolumeSequences / ReadH_BLAST_volinfo,
+ * NF/functions.cpp:573-760) and searches its own length-sorted .hDb copy
+ * (Read_H_BLAST_GPU_DB, NF/functions.cpp:1058-1165, written by makeblastdb
+ * -sort_volumes, NF/writedb_volume.cpp:255-513); these calls read the .psq
+ * directly, so no .hDb and no re-sorted volumes are needed.  Every file is
+ * checked (version, protein type, offset table against the .psq size,
+ * residue total, longest sequence, letters 1..27, 0 bytes exactly between
+ * sequences); a bad file gives HBG_ERR_INVALID and a message naming it.
+ * Subjects are numbered across volumes in DBLIST order. */
+
+/* Counts of a database without reading its sequences (host only). */
+int hbg_blastdb_info(const char *path, int32_t *n_subjects, int64_t *n_residues,
+                     int32_t *max_len, int32_t *n_volumes);
+
+/* Read the sequences into host arrays in hbg_db_open's input form:
+ * residues[n_residues] packed without separators, offsets[n_subjects + 1]. */
+int hbg_blastdb_read(const char *path, uint8_t *residues, int64_t *offsets);
+
+/* Open a resident database straight from the files: each volume's .psq is
+ * streamed to the device through two pinned staging buffers (it already has
+ * the resident layout: a 0 byte, then every sequence followed by a 0 byte).
+ * The result is the same as hbg_db_open on the arrays hbg_blastdb_read
+ * returns. */
+int hbg_db_open_blastdb(const char *path, const hbg_gpu_options *opt, hbg_db **out);
+
 /* ---- query batches -------------------------------------------------------- */
 
 /* Build the neighbourhood lookup tables of a batch of protein queries on the
@@ -285,6 +316,11 @@ typedef struct hbg_server_options {
     int32_t max_batch_queries;   /* queries per batch (default 512) */
     int64_t memory_budget;       /* device bytes for in-flight batches (default 32 GiB) */
     int32_t max_group_len;       /* 0 = library default */
+    int32_t max_batch_letters;   /* query letters per batch, 0 = no cap (default 8192); a
+                                    longer request runs alone */
+    int32_t shortest_first_ms;   /* 0: admit in arrival order.  > 0 (default 2000): requests
+                                    waiting at least this long go first, in arrival order,
+                                    then the shortest waiting requests */
     int32_t pad;
 } hbg_server_options;
 
