@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <numeric>
@@ -727,17 +728,18 @@ int hbg_blastdb_read(const char *path, uint8_t *residues, int64_t *offsets) {
         return rc;
     if (plan.total > 0 && !residues)
         return fail(HBG_ERR_INVALID, "hbg_blastdb_read: null residues");
-    std::vector<uint8_t> buf;
     int64_t at = 0, k = 0;
     offsets[0] = 0;
     for (const hbg::BlastDbVolume &V : plan.vols) {
-        buf.resize((size_t)V.psq_bytes);
-        std::string err = hbg::blastdb_read_psq(V, 0, V.psq_bytes, buf.data());
+        std::unique_ptr<uint8_t[]> buf(new (std::nothrow) uint8_t[(size_t)V.psq_bytes]);   // not zero-filled
+        if (!buf)
+            return fail(HBG_ERR_NOMEM, "host allocation");
+        std::string err = hbg::blastdb_read_psq(V, 0, V.psq_bytes, buf.get());
         if (!err.empty())
             return fail(HBG_ERR_INVALID, err);
         for (int32_t i = 0; i < V.n; ++i) {
             const int64_t L = (int64_t)V.seq_off[i + 1] - V.seq_off[i] - 1;
-            memcpy(residues + at, buf.data() + V.seq_off[i], (size_t)L);
+            memcpy(residues + at, buf.get() + V.seq_off[i], (size_t)L);
             at += L;
             offsets[++k] = at;
         }

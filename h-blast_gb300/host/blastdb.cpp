@@ -20,7 +20,10 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <fcntl.h>
 #include <sys/stat.h>
+#include <thread>
+#include <unistd.h>
 
 namespace hbg {
 
@@ -229,26 +232,62 @@ std::string blastdb_read_psq(const BlastDbVolume &v, int64_t from, int64_t count
     const std::string psq = v.base + ".psq";
     if (from < 0 || count < 0 || from + count > v.psq_bytes)
         return psq + ": read outside the file";
-    FILE *f = fopen(psq.c_str(), "rb");
-    if (!f)
+    const int fd = open(psq.c_str(), O_RDONLY);
+    if (fd < 0)
         return psq + ": cannot be opened";
-    if (fseeko(f, (off_t)from, SEEK_SET) != 0) {
-        fclose(f);
-        return psq + ": seek failed";
+    // large reads are split over a few threads, each reading (pread) and
+    // checking its share: letters in range and the number of 0 bytes
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = count >= (8 << 20) ? (int)std::min(8u, hw) : 1;
+    std::vector<int64_t> zeros_t(nt, 0);
+    std::vector<int> bad_t(nt, 0);         // 1 short read, 2 letter out of range
+    auto work = [&](int t) {
+        const int64_t lo = count * t / nt, hi = count * (t + 1) / nt;
+        int64_t at = lo;
+        while (at < hi) {
+            const ssize_t r = pread(fd, dst + at, (size_t)(hi - at), (off_t)(from + at));
+            if (r <= 0) {
+                bad_t[t] = 1;
+                return;
+            }
+            at += r;
+        }
+        // 4 KiB blocks with narrow accumulators (the compiler vectorises these)
+        uint32_t above = 0;
+        int64_t zeros = 0;
+        for (int64_t b = lo; b < hi; b += 4096) {
+            const int64_t e = std::min<int64_t>(b + 4096, hi);
+            uint8_t ab = 0;
+            uint32_t z = 0;
+            for (int64_t i = b; i < e; ++i) {
+                ab |= (uint8_t)(dst[i] >= kAlphabet);
+                z += dst[i] == 0;
+            }
+            above |= ab;
+            zeros += z;
+        }
+        zeros_t[t] = zeros;
+        if (above)
+            bad_t[t] = 2;
+    };
+    if (nt == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t)
+            th.emplace_back(work, t);
+        for (std::thread &x : th)
+            x.join();
     }
-    const size_t got = count ? fread(dst, 1, (size_t)count, f) : 0;
-    fclose(f);
-    if ((int64_t)got != count)
-        return psq + ": short read";
-    // letters in range, and zeros exactly at the separators in this range
-    uint32_t above = 0;
+    close(fd);
     int64_t zeros = 0;
-    for (int64_t i = 0; i < count; ++i) {
-        above |= (uint32_t)(dst[i] >= kAlphabet);
-        zeros += dst[i] == 0;
+    for (int t = 0; t < nt; ++t) {
+        if (bad_t[t] == 1)
+            return psq + ": short read";
+        if (bad_t[t] == 2)
+            return psq + ": letter outside NCBIstdaa 0..27";
+        zeros += zeros_t[t];
     }
-    if (above)
-        return psq + ": letter outside NCBIstdaa 0..27";
     int64_t seps = 0;
     if (from == 0) {
         if (count > 0 && dst[0] != 0)
