@@ -221,13 +221,13 @@ def served_arm(args):
     out = {"metric": "served latency", "config": {"workload": f"served mixed stream vs {n_sub} subjects "
                                                                f"({ssum} residues)", "requests_per_rate": args.requests}}
     rates = [float(x) for x in args.rates.split(",")]
-    forms = {"served": dict(max_inflight=2, max_batch_queries=512),
-             "served_1": dict(max_inflight=1, max_batch_queries=512),
+    forms = {"served": dict(),
+             "served_2": dict(max_inflight=2),
              "served_fifo": dict(max_inflight=2, max_batch_queries=512, max_batch_letters=0, shortest_first_ms=0),
              "plain": dict(max_inflight=1, max_batch_queries=1, max_batch_letters=0, shortest_first_ms=0)}
     out["forms"] = {"served": "library defaults: shortest-first admission (age bound 2 s), <= 8192 query "
-                              "letters per batch, 2 batches in flight",
-                    "served_1": "as served, 1 batch in flight (the next batch is chosen when one ends)",
+                              "letters per batch, 1 batch in flight (the next is chosen when one ends)",
+                    "served_2": "as served, 2 batches in flight",
                     "served_fifo": "arrival-order admission, no letter cap, 2 batches in flight",
                     "plain": "one query per launch, one at a time, arrival order"}
     for form, so in forms.items():

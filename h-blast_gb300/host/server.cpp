@@ -273,7 +273,7 @@ extern "C" {
 int hbg_server_default_options(hbg_server_options *o) {
     if (!o)
         return HBG_ERR_INVALID;
-    o->max_inflight = 2;
+    o->max_inflight = 1;
     o->max_batch_queries = 512;
     o->memory_budget = (int64_t)32 << 30;
     o->max_group_len = 0;

@@ -312,7 +312,8 @@ int hbg_result_free(hbg_result *res);
 typedef struct hbg_server hbg_server;
 
 typedef struct hbg_server_options {
-    int32_t max_inflight;        /* searches in flight (default 2) */
+    int32_t max_inflight;        /* searches in flight (default 1: the next batch is chosen
+                                    when one ends, from everything then waiting) */
     int32_t max_batch_queries;   /* queries per batch (default 512) */
     int64_t memory_budget;       /* device bytes for in-flight batches (default 32 GiB) */
     int32_t max_group_len;       /* 0 = library default */
