@@ -14,6 +14,9 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
+#include <functional>
+#include <thread>
 
 namespace hbg {
 
@@ -37,6 +40,8 @@ class NeighbourCache {
         lists_.resize(HBG_NUM_CELLS);
     }
 
+    // Read-only once every word in use has been enumerated (prepare()), so
+    // several threads may call it.
     const std::vector<uint16_t> &get(uint8_t a, uint8_t b, uint8_t c) {
         int32_t key = (a << 10) | (b << 5) | c;
         if (!done_[key]) {
@@ -44,6 +49,21 @@ class NeighbourCache {
             done_[key] = 1;
         }
         return lists_[key];
+    }
+
+    // Enumerate the neighbourhoods of the flagged words, in parallel.
+    template <typename ParallelFor>
+    void prepare(const std::vector<uint8_t> &need, ParallelFor &&pfor) {
+        std::vector<int32_t> keys;
+        for (int32_t k = 0; k < HBG_NUM_CELLS; ++k)
+            if (need[k] && !done_[k])
+                keys.push_back(k);
+        pfor((int64_t)keys.size(), [&](int64_t i) {
+            const int32_t k = keys[i];
+            enumerate((uint8_t)(k >> 10), (uint8_t)((k >> 5) & 31), (uint8_t)(k & 31), &lists_[k]);
+        });
+        for (int32_t k : keys)
+            done_[k] = 1;
     }
 
   private:
@@ -71,6 +91,28 @@ class NeighbourCache {
     std::vector<uint8_t> done_;
     std::vector<std::vector<uint16_t>> lists_;
 };
+
+// Run body(i) for i in [0, n) on up to 16 host threads (items taken from a
+// shared counter).
+void parallel_for(int64_t n, const std::function<void(int64_t)> &body) {
+    const int64_t nt = std::min<int64_t>({n, 16, (int64_t)std::max(1u, std::thread::hardware_concurrency())});
+    if (nt <= 1) {
+        for (int64_t i = 0; i < n; ++i)
+            body(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    auto run = [&] {
+        for (int64_t i = next++; i < n; i = next++)
+            body(i);
+    };
+    std::vector<std::thread> th;
+    for (int64_t t = 1; t < nt; ++t)
+        th.emplace_back(run);
+    run();
+    for (std::thread &x : th)
+        x.join();
+}
 
 int32_t next_pow2(int32_t v) {
     int32_t n = 1;
@@ -206,20 +248,37 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
     b.cells.assign((size_t)n_groups * HBG_CELL_STRIDE, 0);
     b.pv.assign((size_t)n_groups * HBG_PV_WORDS, 0);
     b.query_cells.assign(qs.size() * (size_t)HBG_NUM_CELLS, 0);
-    std::vector<uint32_t> count(HBG_NUM_CELLS);
-    int64_t entry_pos = 0;
-    for (int32_t g = 0; g < n_groups; ++g) {
+    // the neighbourhoods of every word in the batch, enumerated in parallel;
+    // then per group (in parallel: groups own disjoint cells, queries and
+    // entries) count, prefix, and fill
+    auto valid = [&](const int32_t *gc, int32_t p) {
+        const int32_t c0 = gc[p];
+        return c0 >= 0 && gc[p + 1] == c0 && gc[p + 2] == c0;
+    };
+    {
+        std::vector<uint8_t> need(HBG_NUM_CELLS, 0);
+        for (int32_t g = 0; g < n_groups; ++g) {
+            const HbgGroup &G = b.groups[g];
+            const uint8_t *gs = b.letters.data() + G.seq_base;
+            const int32_t *gc = b.ctx_of.data() + G.seq_base;
+            for (int32_t p = 0; p + HBG_WORD_SIZE <= G.glen; ++p)
+                if (valid(gc, p))
+                    need[(gs[p] << 10) | (gs[p + 1] << 5) | gs[p + 2]] = 1;
+        }
+        nb.prepare(need, parallel_for);
+    }
+    std::vector<uint32_t> group_entries(n_groups, 0);
+    parallel_for(n_groups, [&](int64_t gi) {
+        const int32_t g = (int32_t)gi;
         HbgGroup &G = b.groups[g];
         const uint8_t *gs = b.letters.data() + G.seq_base;
         const int32_t *gc = b.ctx_of.data() + G.seq_base;
-        std::fill(count.begin(), count.end(), 0);
-        // count
+        std::vector<uint32_t> count(HBG_NUM_CELLS, 0);
         for (int32_t p = 0; p + HBG_WORD_SIZE <= G.glen; ++p) {
-            int32_t c0 = gc[p];
-            if (c0 < 0 || gc[p + 1] != c0 || gc[p + 2] != c0)
+            if (!valid(gc, p))
                 continue;
             const std::vector<uint16_t> &ws = nb.get(gs[p], gs[p + 1], gs[p + 2]);
-            uint16_t *qc = b.query_cells.data() + (size_t)b.contexts[c0].query * HBG_NUM_CELLS;
+            uint16_t *qc = b.query_cells.data() + (size_t)b.contexts[gc[p]].query * HBG_NUM_CELLS;
             for (uint16_t w : ws) {
                 ++count[w];
                 ++qc[w];
@@ -235,33 +294,41 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
                 pv[w >> 5] |= 1u << (w & 31);
         }
         cs[HBG_NUM_CELLS] = acc;
-        G.entry_base = entry_pos;
+        group_entries[g] = acc;
         // expected hits per subject offset on typical proteins: entries of
         // words over the 20 standard letters, each such word taken as
         // equally likely (1 / 8000)
-        {
-            static const uint8_t kStd[20] = {1, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 22};
-            uint64_t std_entries = 0;
-            for (int x = 0; x < 20; ++x)
-                for (int y = 0; y < 20; ++y)
-                    for (int z = 0; z < 20; ++z)
-                        std_entries += count[(kStd[x] << 10) | (kStd[y] << 5) | kStd[z]];
-            G.mode = (double)std_entries / 8000.0 >= mode_hits ? 1 : 0;
-        }
-        b.entries.resize((size_t)(entry_pos + acc));
-        // fill (ascending p inside each cell)
+        static const uint8_t kStd[20] = {1, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 22};
+        uint64_t std_entries = 0;
+        for (int x = 0; x < 20; ++x)
+            for (int y = 0; y < 20; ++y)
+                for (int z = 0; z < 20; ++z)
+                    std_entries += count[(kStd[x] << 10) | (kStd[y] << 5) | kStd[z]];
+        G.mode = (double)std_entries / 8000.0 >= mode_hits ? 1 : 0;
+    });
+    int64_t entry_pos = 0;
+    for (int32_t g = 0; g < n_groups; ++g) {
+        b.groups[g].entry_base = entry_pos;
+        entry_pos += group_entries[g];
+    }
+    b.entries.resize((size_t)entry_pos);
+    parallel_for(n_groups, [&](int64_t gi) {
+        const int32_t g = (int32_t)gi;
+        const HbgGroup &G = b.groups[g];
+        const uint8_t *gs = b.letters.data() + G.seq_base;
+        const int32_t *gc = b.ctx_of.data() + G.seq_base;
+        const uint32_t *cs = b.cells.data() + (size_t)g * HBG_CELL_STRIDE;
+        // fill, ascending p inside each cell
         std::vector<uint32_t> cursor(cs, cs + HBG_NUM_CELLS);
-        uint16_t *ge = b.entries.data() + entry_pos;
+        uint16_t *ge = b.entries.data() + G.entry_base;
         for (int32_t p = 0; p + HBG_WORD_SIZE <= G.glen; ++p) {
-            int32_t c0 = gc[p];
-            if (c0 < 0 || gc[p + 1] != c0 || gc[p + 2] != c0)
+            if (!valid(gc, p))
                 continue;
             const std::vector<uint16_t> &ws = nb.get(gs[p], gs[p + 1], gs[p + 2]);
             for (uint16_t w : ws)
                 ge[cursor[w]++] = (uint16_t)p;
         }
-        entry_pos += acc;
-    }
+    });
     return std::string();
 }
 
