@@ -255,19 +255,28 @@ int plan_launches(const hbg_batch *b, const hbg_gpu_options &o, int device, std:
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     out->clear();
     for (const LaunchClass &lc : b->classes) {
-        int t = o.num_threadsx;
-        while (t > 32 && hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
-            t = ((t / 2) + 31) / 32 * 32;
-        if (hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
-            return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
-        int blocks = o.num_blocksx;
-        if (blocks <= 0) {
-            int per = 1;
+        // num_threadsx is the largest CTA size: per class take the size (halving
+        // down to 64) that keeps the most warps resident per SM -- large diagonal
+        // tables fill shared memory, and smaller CTAs pack it better
+        int best_t = 0, best_per = 0, best_warps = -1;
+        for (int t = o.num_threadsx; t >= 32; t = t > 64 ? ((t / 2) + 31) / 32 * 32 : 0) {
+            if (hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
+                continue;
+            int per = 0;
             if (hbg::wordfinder_occupancy(lc.mode, t, lc.smem_diag, &per) != cudaSuccess || per < 1)
                 per = 1;
-            blocks = sms * per;
+            if (per * (t / 32) > best_warps) {
+                best_t = t;
+                best_per = per;
+                best_warps = per * (t / 32);
+            }
+            if (o.num_blocksx > 0)
+                break;                 // a fixed grid keeps the caller's CTA size when it fits
         }
-        out->push_back(LaunchShape{t, blocks});
+        if (best_t == 0)
+            return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
+        const int blocks = o.num_blocksx > 0 ? o.num_blocksx : sms * best_per;
+        out->push_back(LaunchShape{best_t, blocks});
     }
     return HBG_OK;
 }

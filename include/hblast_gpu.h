@@ -92,9 +92,12 @@ typedef struct hbg_word_params {
 
 /* Mirror of BlastGPUOptions (NF/blast_options.h:503-514), the values of the
  * -gpu, -gpu_threads, -gpu_blocks, -method and -num_threads flags
- * (NF/blast_args.cpp:2705-2778).  num_threadsx is the CTA size (a multiple
- * of 32, 32..1024); num_blocksx 0 means one persistent wave sized from the
- * SM count; method selects the device among the visible ones (0 = first);
+ * (NF/blast_args.cpp:2705-2778).  num_threadsx is the largest CTA size (a
+ * multiple of 32, 32..1024): with num_blocksx 0 (one persistent wave sized
+ * from the SM count) each launch uses the size, halving down to 64, that
+ * keeps the most warps resident (large diagonal tables fill shared memory);
+ * with num_blocksx > 0 both are used as given when they fit.  method selects
+ * the device among the visible ones (0 = first);
  * use_gpu 0 makes hbg_search return HBG_ERR_NO_DEVICE (this library has no
  * CPU path). */
 typedef struct hbg_gpu_options {
