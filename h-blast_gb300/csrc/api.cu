@@ -145,7 +145,8 @@ struct hbg_result {
     hbg_gpu_options shape_opt{};     // options the shapes were computed for
     // device
     hbg_hsp *d_raw = nullptr, *d_sorted = nullptr;
-    unsigned long long *d_counters = nullptr;  // [0]=hsp count, then per query ext, kept, hits; per group hits
+    unsigned long long *d_counters = nullptr;  // [0]=hsp count, then per query ext, kept, hits; per group
+                                               // hits; per query first, end of its HSPs, subjects passed
     unsigned int *d_tile = nullptr;
     uint32_t *d_gdiag = nullptr;
     int64_t gdiag_entries = 0;
@@ -158,7 +159,6 @@ struct hbg_result {
     // host
     unsigned long long *h_counters = nullptr;  // pinned
     size_t n_counters = 0;
-    std::vector<hbg_hsp> hsps;
     std::vector<hbg_query_stats> stats;
     std::vector<int64_t> q_first, q_count;
     int64_t n_hsps = 0;
@@ -313,12 +313,12 @@ int prepare_result(hbg_result *r, int64_t cap) {
         for (auto &e : r->ev)
             CU(cudaEventCreate(&e));
     }
-    if (r->n_counters < 1 + 3 * nq + ng) {   // first use, or a larger batch
+    if (r->n_counters < 1 + 6 * nq + ng) {   // first use, or a larger batch
         dfree(r->d_counters);
         if (r->h_counters)
             cudaFreeHost(r->h_counters);
         r->h_counters = nullptr;
-        r->n_counters = 1 + 3 * nq + ng;
+        r->n_counters = 1 + 6 * nq + ng;
         CU(dalloc(&r->d_counters, r->n_counters));
         CU(cudaMallocHost((void **)&r->h_counters, r->n_counters * sizeof(unsigned long long)));
     }
@@ -427,12 +427,15 @@ int enqueue_search(hbg_result *r) {
     o.bits_s = bits_for((int64_t)db->n - 1);
     o.bits_so = bits_for(db->max_len);
     o.bits_qo = bits_for(h.max_query_len);
+    o.q_first = r->d_counters + 1 + 3 * nq + ng;
+    o.q_end = o.q_first + nq;
+    o.q_passed = o.q_end + nq;
     if (o.bits_q + o.bits_s + o.bits_so + o.bits_qo > 64)
         return fail(HBG_ERR_TOO_LONG, "ordering key exceeds 64 bits for this database and batch");
     CU(hbg::launch_order(o, st));
     {
         const int bits = o.bits_q + o.bits_s + o.bits_so + o.bits_qo;
-        r->launches = (db->n > 0 ? (int32_t)b->classes.size() : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 2 + 3 * ((bits + 7) / 8) : 0) +
+        r->launches = (db->n > 0 ? (int32_t)b->classes.size() : 0) + (hbg::order_max_blocks(r->cap) > 0 ? 3 + 3 * ((bits + 7) / 8) : 0) +
                       (nq > 0 ? 1 : 0);
     }
     CU(hbg::launch_query_hits(db->d_hist, b->d_qcells, (int32_t)nq, r->d_counters + 1 + 2 * nq, st));
@@ -1214,12 +1217,10 @@ int hbg_result_wait(hbg_result *r) {
         return rc;
     if (r->done)
         return HBG_OK;
-    DeviceScope ds(r->device);
-    const int64_t n = r->n_hsps;
-    r->hsps.resize((size_t)n);
-    if (n)
-        CU(cudaMemcpy(r->hsps.data(), r->d_sorted, (size_t)n * sizeof(hbg_hsp), cudaMemcpyDeviceToHost));
-    const size_t nq = r->batch->host.queries.size();
+    // the ordered HSPs stay on the device (read with hbg_result_hsps); the
+    // ordering pass left per-query ranges and subject counts beside the counters
+    const size_t nq = r->batch->host.queries.size(), ng = r->batch->host.groups.size();
+    const unsigned long long *rng = r->h_counters + 1 + 3 * nq + ng;
     r->stats.assign(nq, hbg_query_stats{0, 0, 0, 0});
     r->q_first.assign(nq, 0);
     r->q_count.assign(nq, 0);
@@ -1227,15 +1228,9 @@ int hbg_result_wait(hbg_result *r) {
         r->stats[q].init_extends = (int64_t)r->h_counters[1 + q];
         r->stats[q].good_init_extends = (int64_t)r->h_counters[1 + nq + q];
         r->stats[q].lookup_hits = (int64_t)r->h_counters[1 + 2 * nq + q];
-    }
-    // per-query ranges and subjects with HSPs (the list is ordered by query, subject)
-    for (int64_t i = 0; i < (int64_t)n; ++i) {
-        const hbg_hsp &h = r->hsps[(size_t)i];
-        if (r->q_count[h.query] == 0)
-            r->q_first[h.query] = i;
-        r->q_count[h.query]++;
-        if (i == 0 || r->hsps[(size_t)i - 1].query != h.query || r->hsps[(size_t)i - 1].subject != h.subject)
-            r->stats[h.query].subjects_passed++;
+        r->stats[q].subjects_passed = (int64_t)rng[2 * nq + q];
+        r->q_first[q] = (int64_t)rng[q];
+        r->q_count[q] = (int64_t)rng[nq + q] - (int64_t)rng[q];
     }
     r->done = true;
     return HBG_OK;
@@ -1268,8 +1263,14 @@ int hbg_result_hsps(const hbg_result *r, int64_t first, int64_t count, hbg_hsp *
         return fail(HBG_ERR_STATE, "result not collected");
     if (first < 0 || count < 0 || first + count > r->n_hsps || (count > 0 && !out))
         return fail(HBG_ERR_INVALID, "range outside the result");
-    if (count)
-        memcpy(out, r->hsps.data() + first, (size_t)count * sizeof(hbg_hsp));
+    if (count) {
+        // on the search's own stream, so the copy neither waits for nor races
+        // with work on other streams
+        DeviceScope ds(r->device);
+        CU(cudaMemcpyAsync(out, r->d_sorted + first, (size_t)count * sizeof(hbg_hsp), cudaMemcpyDeviceToHost,
+                           r->stream));
+        CU(cudaStreamSynchronize(r->stream));
+    }
     return HBG_OK;
 }
 
@@ -1320,8 +1321,15 @@ int hbg_search_sync(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, hb
         if (out) {
             if (r->n_hsps > out_cap)
                 rc = fail(HBG_ERR_CAPACITY, "output buffer too small");
-            else if (r->n_hsps)
-                memcpy(out, r->hsps.data(), (size_t)r->n_hsps * sizeof(hbg_hsp));
+            else if (r->n_hsps) {
+                DeviceScope ds(r->device);
+                cudaError_t e = cudaMemcpyAsync(out, r->d_sorted, (size_t)r->n_hsps * sizeof(hbg_hsp),
+                                                cudaMemcpyDeviceToHost, r->stream);
+                if (e == cudaSuccess)
+                    e = cudaStreamSynchronize(r->stream);
+                if (e != cudaSuccess)
+                    rc = fail(HBG_ERR_CUDA, std::string("cudaMemcpy (HSPs): ") + cudaGetErrorString(e));
+            }
         }
     }
     hbg_result_free(r);

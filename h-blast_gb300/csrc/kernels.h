@@ -66,6 +66,9 @@ struct OrderArgs {
     uint32_t *vals[2];
     uint32_t *hist;                   // 256 x max_blocks
     int bits_q, bits_s, bits_so, bits_qo;
+    // optional (null = skip): per-query first / end index in `out` and the
+    // number of subjects with HSPs, each n_queries entries, zeroed beforehand
+    unsigned long long *q_first, *q_end, *q_passed;
 };
 int64_t order_max_blocks(int64_t cap);
 cudaError_t launch_order(const OrderArgs &a, cudaStream_t stream);

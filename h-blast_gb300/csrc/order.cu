@@ -162,6 +162,26 @@ __global__ void gather_hsps(const hbg_hsp *in, const uint32_t *vals,
         out[i] = in[vals[i]];
 }
 
+// Per-query ranges of the ordered list (sorted by query, then subject):
+// first[q] and end[q] bound query q's HSPs, passed[q] counts its subjects
+// with at least one HSP.  All three start at zero.
+__global__ void query_ranges(const hbg_hsp *sorted, const unsigned long long *count, int64_t cap,
+                             unsigned long long *first, unsigned long long *end,
+                             unsigned long long *passed) {
+    const int64_t n = live_count(count, cap);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t q = sorted[i].query, s = sorted[i].subject;
+        const bool new_q = i == 0 || sorted[i - 1].query != q;
+        if (new_q)
+            first[q] = (unsigned long long)i;
+        if (i == n - 1 || sorted[i + 1].query != q)
+            end[q] = (unsigned long long)(i + 1);
+        if (new_q || sorted[i - 1].subject != s)
+            atomicAdd(passed + q, 1ull);
+    }
+}
+
 __global__ void __launch_bounds__(256)
 db_histogram(const uint8_t *db, int64_t n, unsigned long long *hist) {
     extern __shared__ unsigned int hsm[];
@@ -221,6 +241,8 @@ cudaError_t launch_order(const OrderArgs &a, cudaStream_t stream) {
         src ^= 1;
     }
     gather_hsps<<<gblocks, 256, 0, stream>>>(a.in, a.vals[src], a.count, a.cap, a.out);
+    if (a.q_first)
+        query_ranges<<<gblocks, 256, 0, stream>>>(a.out, a.count, a.cap, a.q_first, a.q_end, a.q_passed);
     return cudaGetLastError();
 }
 

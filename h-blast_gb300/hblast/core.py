@@ -388,7 +388,7 @@ class Searcher:
 
     def result(self) -> SearchResult:
         n = self.n_hsps()
-        out = np.zeros(n, dtype=HSP_DTYPE)
+        out = np.empty(n, dtype=HSP_DTYPE)
         if n:
             _check(lib().hbg_result_hsps(self.res, 0, n, out.ctypes.data))
         stats = []

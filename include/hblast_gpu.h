@@ -271,16 +271,17 @@ int hbg_mem_required(const hbg_db *db, const hbg_batch *batch, int64_t hsp_capac
 int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt,
                int64_t hsp_capacity, void *stream, hbg_result **out);
 
-/* Wait for the search, put HSPs in reference order -- by query, then subject,
- * then the order the CPU word finder creates them (subject offset, then
- * query offset) -- and copy them to the host.  Replaces H_BLAST_get_data +
- * memory_defrag (h_blast.cu:1160-1252). */
+/* Wait for the search and collect it: HSPs in reference order -- by query,
+ * then subject, then the order the CPU word finder creates them (subject
+ * offset, then query offset) -- with per-query ranges, counters and subjects
+ * passed (all computed on the device).  The ordered HSPs stay in device
+ * memory until the result is relaunched or freed; hbg_result_hsps copies any
+ * range of them to the host.  Replaces H_BLAST_get_data + memory_defrag
+ * (h_blast.cu:1160-1252). */
 int hbg_result_wait(hbg_result *res);
 
-/* Wait for the search and read its counters and timings without copying the
- * HSPs to the host (they stay ordered in device memory); hbg_result_wait may
- * follow to copy them.  Relaunches on HSP-buffer overflow like
- * hbg_result_wait. */
+/* Wait for the search and read its HSP count and timings only; relaunches on
+ * HSP-buffer overflow like hbg_result_wait. */
 int hbg_result_sync(hbg_result *res);
 
 /* Device time of the word-finder kernel and of the ordering pass, in ms,
@@ -290,7 +291,8 @@ int hbg_result_timing(const hbg_result *res, float *wordfinder_ms, float *orderi
 
 int hbg_result_counts(const hbg_result *res, int64_t *n_hsps, int32_t *n_queries);
 
-/* Copy HSPs [first, first+count) of the ordered list. */
+/* Copy HSPs [first, first+count) of the ordered list from device memory to
+ * `out` (host), on the search's stream. */
 int hbg_result_hsps(const hbg_result *res, int64_t first, int64_t count, hbg_hsp *out);
 
 /* Range of query q in the ordered list: HSPs [*first, *first + *count). */
