@@ -404,6 +404,12 @@ int enqueue_search(hbg_result *r) {
     if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
         for (size_t c = 0; c < b->classes.size(); ++c) {
             const LaunchClass &lc = b->classes[c];
+            // tiles of up to 128 subjects, fewer when a class has too little
+            // work to give every CTA about eight tiles (small databases and
+            // single queries would otherwise leave most SMs idle)
+            const int64_t want = (int64_t)db->n * lc.count / (8 * (int64_t)r->shapes[c].blocks);
+            a.tile_subjects = (int32_t)std::max<int64_t>(8, std::min<int64_t>(128, want));
+            a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
             a.group_list = b->d_group_list + lc.first;
             a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
             a.tile_counter = r->d_tile + c;
