@@ -131,6 +131,7 @@ struct hbg_batch {
     int32_t *d_group_list = nullptr;   // groups ordered by launch class
     std::vector<LaunchClass> classes;
     int64_t device_bytes = 0;
+    int32_t tile_subjects = 0;   // 0 = automatic (hbg_batch_tune)
 };
 
 struct hbg_result {
@@ -419,7 +420,8 @@ int enqueue_search(hbg_result *r) {
             // work to give every CTA about eight tiles (small databases and
             // single queries would otherwise leave most SMs idle)
             const int64_t want = (int64_t)db->n * lc.count / (8 * (int64_t)r->shapes[c].blocks);
-            a.tile_subjects = (int32_t)std::max<int64_t>(8, std::min<int64_t>(128, want));
+            a.tile_subjects = b->tile_subjects > 0 ? b->tile_subjects
+                                                   : (int32_t)std::max<int64_t>(8, std::min<int64_t>(128, want));
             a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
             a.group_list = b->d_group_list + lc.first;
             a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
@@ -1062,6 +1064,29 @@ int hbg_batch_set_mode(hbg_batch *b, int32_t g, int32_t mode) {
     for (int32_t i = 0; i < (int32_t)b->host.groups.size(); ++i)
         if (g < 0 || i == g)
             b->host.groups[i].mode = mode;
+    return HBG_OK;
+}
+
+int hbg_batch_tune(hbg_batch *b, int32_t tile_subjects, int32_t global_tables) {
+    if (!b || tile_subjects < 0 || (tile_subjects > 0 && (tile_subjects < 8 || tile_subjects > 4096)) ||
+        (global_tables != 0 && global_tables != 1))
+        return fail(HBG_ERR_INVALID, "hbg_batch_tune: bad argument");
+    if (b->device >= 0)
+        return fail(HBG_ERR_STATE, "batch already uploaded: tune before the first search");
+    b->tile_subjects = tile_subjects;
+    if (global_tables) {
+        hbg::HostBatch &h = b->host;
+        for (HbgGroup &G : h.groups) {
+            if (G.placement)
+                continue;
+            int32_t n = 1;
+            while (n < G.glen + h.window)
+                n <<= 1;
+            G.diag_len = n;                      // global tables are powers of two
+            G.placement = 1;
+            h.max_diag_len = std::max(h.max_diag_len, G.diag_len);
+        }
+    }
     return HBG_OK;
 }
 

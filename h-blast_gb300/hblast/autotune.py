@@ -1,6 +1,10 @@
 """Autotuner for the word finder: per query-length bucket, choose the query
-group length, the hit mode (chunk mode / offset mode) and the CTA size by
-timing searches of the bucket's queries against a sample of the database.
+group length, the hit mode (chunk mode / offset mode), the CTA size, the
+subjects per work unit (the subject chunk a CTA takes: 32, 128 or 512
+subjects, about 11, 46 or 184 KB of letters) and the diagonal-table placement
+(shared or global memory) by timing searches of the bucket's queries against
+a sample of the database.  Stage one times the group-length / mode / CTA
+candidates; stage two varies the work unit and the placement of the best.
 
 Every choice gives identical HSPs (the tests check it); only time changes.
 The report lists, per bucket and candidate, the word-finder time, the
@@ -11,7 +15,7 @@ with the chosen settings and merges the results in reference order.
 from __future__ import annotations
 
 import json
-from dataclasses import asdict, dataclass, field
+from dataclasses import asdict, dataclass, field, replace
 from pathlib import Path
 from typing import Sequence
 
@@ -26,13 +30,16 @@ DEFAULT_BUCKETS = ((0, 300), (300, 1000), (1000, 4000), (4000, 65001))
 class Choice:
     max_group_len: int      # 1 = one query per group; 0 = library default
     mode: int               # 0 chunk mode, 1 offset mode
-    threads: int            # CTA size
+    threads: int            # largest CTA size
+    tile_subjects: int = 0  # subjects per work unit, 0 = automatic
+    global_tables: bool = False
 
 
 DEFAULT_CANDIDATES = (
     Choice(1, 0, 256), Choice(1000, 0, 256), Choice(2008, 0, 256), Choice(2008, 0, 128),
     Choice(4056, 0, 128), Choice(8152, 1, 256), Choice(16344, 1, 128),
 )
+STAGE2 = (dict(tile_subjects=32), dict(tile_subjects=128), dict(tile_subjects=512), dict(global_tables=True))
 
 
 @dataclass
@@ -47,6 +54,7 @@ class BucketResult:
 def time_choice(db: core.Database, pqs: Sequence[core.ProteinQuery], choice: Choice, db_residues: int,
                 reps: int = 2) -> float:
     batch = core.Batch.proteins(pqs, max_group_len=choice.max_group_len).set_mode(choice.mode)
+    batch.tune(choice.tile_subjects, choice.global_tables)
     s = core.Searcher(db, batch, core.default_options(num_threadsx=choice.threads))
     try:
         best = float("inf")
@@ -61,7 +69,9 @@ def time_choice(db: core.Database, pqs: Sequence[core.ProteinQuery], choice: Cho
 
 
 def tune(db: core.Database, queries: Sequence[core.ProteinQuery], db_residues: int,
-         buckets=DEFAULT_BUCKETS, candidates=DEFAULT_CANDIDATES, reps: int = 2) -> list[BucketResult]:
+         buckets=DEFAULT_BUCKETS, candidates=DEFAULT_CANDIDATES, reps: int = 2,
+         stage2=STAGE2) -> list[BucketResult]:
+    """Rows per bucket: (choice, word-finder ms, subject-stream GB/s, query x db residues/s)."""
     out = []
     for lo, hi in buckets:
         pqs = [q for q in queries if lo <= q.length < hi]
@@ -69,12 +79,20 @@ def tune(db: core.Database, queries: Sequence[core.ProteinQuery], db_residues: i
         if pqs:
             qres = sum(q.length for q in pqs)
             best_ms = float("inf")
-            for c in candidates:
+
+            def measure(c):
+                nonlocal best_ms
                 ms = time_choice(db, pqs, c, db_residues, reps)
                 gbs = db_residues / (ms * 1e-3) / 1e9
                 br.rows.append((asdict(c), ms, gbs, qres * db_residues / (ms * 1e-3)))
                 if ms < best_ms:
                     best_ms, br.best = ms, c
+
+            for c in candidates:
+                measure(c)
+            first = br.best
+            for kw in stage2:
+                measure(replace(first, **kw))
         out.append(br)
     return out
 
@@ -110,6 +128,7 @@ def search_tuned(db: core.Database, queries: Sequence[core.ProteinQuery],
     wf = od = 0.0
     for c, idx in by_choice.items():
         batch = core.Batch.proteins([queries[i] for i in idx], max_group_len=c.max_group_len).set_mode(c.mode)
+        batch.tune(c.tile_subjects, c.global_tables)
         r = core.search(db, batch, core.default_options(num_threadsx=c.threads))
         h = r.hsps.copy()
         h["query"] = np.asarray(idx, dtype=np.int32)[h["query"]]

@@ -77,6 +77,7 @@ _SIGS = {
     "hbg_read_runtime_options": ([C.c_char_p, C.POINTER(RuntimeOptions)], C.c_int),
     "hbg_db_open": ([_P, _P, C.c_int32, C.POINTER(GpuOptions), C.POINTER(_P)], C.c_int),
     "hbg_db_close": ([_P], C.c_int),
+    "hbg_batch_tune": ([_P, C.c_int32, C.c_int32], C.c_int),
     "hbg_blastdb_info": ([C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                           C.POINTER(C.c_int32)], C.c_int),
     "hbg_blastdb_read": ([C.c_char_p, _P, _P], C.c_int),
@@ -325,6 +326,11 @@ class Batch:
         _check(lib().hbg_batch_lookup_table(self.handle, g, cells.ctypes.data, ent.ctypes.data, len(ent),
                                             C.byref(n), C.byref(fq), C.byref(nq), qs.ctypes.data))
         return cells, ent[:n.value], fq.value, qs[:nq.value]
+
+    def tune(self, tile_subjects: int = 0, global_tables: bool = False) -> "Batch":
+        """hbg_batch_tune: subjects per work unit (0 = automatic), diagonal tables in global memory."""
+        _check(lib().hbg_batch_tune(self.handle, tile_subjects, int(global_tables)))
+        return self
 
     def set_mode(self, mode: int, group: int = -1) -> "Batch":
         """0 = chunk mode, 1 = offset mode, for one group or all (before the first search)."""

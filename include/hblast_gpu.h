@@ -245,6 +245,16 @@ int hbg_batch_lookup_table(const hbg_batch *batch, int32_t g, uint32_t *cells,
  * not depend on the choice.  Call before the batch's first search. */
 int hbg_batch_set_mode(hbg_batch *batch, int32_t g, int32_t mode);
 
+/* Work-unit and table placement knobs for tuning (results do not depend on
+ * them).  tile_subjects: subjects per work unit a CTA takes (8..4096; 0 =
+ * automatic: 128, fewer when the work is small); with the benchmark's length
+ * law a tile of 128 subjects is about 46 KB of subject letters.
+ * global_tables 1: every group keeps its diagonal table (32-bit cells) in
+ * global memory instead of shared memory.  Call before the batch's first
+ * search.  (H-BLAST fixes these at compile time: its per-thread diagonal
+ * arrays are global, h_blast_kernel.cu:603-630.) */
+int hbg_batch_tune(hbg_batch *batch, int32_t tile_subjects, int32_t global_tables);
+
 int hbg_batch_destroy(hbg_batch *batch);
 /* Sizes of a batch; device_bytes is what its upload copies host-to-device. */
 int hbg_batch_info(const hbg_batch *batch, int32_t *n_queries, int32_t *n_groups,
