@@ -210,9 +210,10 @@ int upload_batch(hbg_batch *b, int device) {
     {
         // launch classes: (mode, table size bucket); tables of <= 2048 entries
         // share one class (they all allow four CTAs per SM); larger shared
-        // tables (exact lengths) are bucketed and each class allocates its
-        // longest member; global-table groups form their own class per mode
-        static const int kBuckets[] = {2560, 3072, 4096, 5120, 6144, 8192, 10240, 12288, 16384};
+        // tables (exact lengths, up to 4096) are bucketed and each class
+        // allocates its longest member; global-table groups form their own
+        // class per mode
+        static const int kBuckets[] = {2560, 3072, 4096};   // shared tables end at kSmemDiagMax
         std::vector<std::pair<std::pair<int, int>, int32_t>> keyed;
         for (int32_t g = 0; g < (int32_t)h.groups.size(); ++g) {
             const HbgGroup &G = h.groups[g];
@@ -1444,7 +1445,7 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
         return fail(HBG_ERR_TOO_LONG, "hbg_search_static: the batch needs " + std::to_string(need) +
                                           " scratch bytes, more than HBG_STATIC_SCRATCH_BYTES");
     if (global_diag_len(h, db) > 0)
-        return fail(HBG_ERR_TOO_LONG, "hbg_search_static: groups longer than 16344 letters or subjects "
+        return fail(HBG_ERR_TOO_LONG, "hbg_search_static: groups longer than 4056 letters or subjects "
                                       "longer than 32767 - window need global diagonal tables");
     DeviceScope ds(db->device);
     void *scratch = nullptr;

@@ -15,7 +15,11 @@ namespace hbg {
 
 // Shared-memory diagonal tables (16-bit cells) hold at most this many
 // entries per warp; groups whose table is longer use the global scratch.
-constexpr int32_t kSmemDiagMax = 16384;
+// Measured on GB300: up to ~4096 entries shared tables are as fast or
+// faster; beyond, their footprint cuts resident warps to 8-12 per SM and
+// 32-bit tables in global memory (L2-resident, 32 warps per SM) are 17-23 %
+// faster (groups of 5000 to 15000 letters, and six-frame BLASTX queries).
+constexpr int32_t kSmemDiagMax = 4096;
 // Default group length: the table of a full group is 2048 entries (4 KB), small
 // enough for four 8-warp CTAs per SM.
 constexpr int32_t kDefaultGroupTable = 2048;

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 def test_tuned_search_equals_default(built, tmp_path):
     rng = np.random.default_rng(51)
     qs = synth.heavy_tailed_queries(3, 24)
-    qs[0] = synth.random_letters(rng, 9000)           # a long query (16384-entry table)
+    qs[0] = synth.random_letters(rng, 9000)           # a long query (16384-entry global table)
     db = synth.make_db(rng, 3000, 300, 0.6, 30, 5000, 0.05, qs, lambda r: r.integers(50, 301), 0.5)
     gdb = hblast.Database(db.residues, db.offsets)
     pqs = [hblast.ProteinQuery.blastp(q) for q in qs]

@@ -74,10 +74,10 @@ def test_alone_equals_in_the_mix(small_db):
         assert np.array_equal(got, alone), k
 
 
-@pytest.mark.parametrize("qlen", [9000, 20000])
+@pytest.mark.parametrize("qlen", [3000, 9000, 20000])
 def test_long_query_tables(built, qlen):
-    # 9000: a 16384-entry shared table (4-warp CTAs); 20000: a 32768-entry
-    # table in the global scratch
+    # 3000: an exact-length shared table (3040 entries, indexed by remainder);
+    # 9000 and 20000: 16384- and 32768-entry tables in the global scratch
     rng = np.random.default_rng(12)
     q = synth.random_letters(rng, qlen)
     db = synth.make_db(rng, 300, 300, 0.6, 30, 5000, 40, [q], lambda r: r.integers(100, 400), 0.5)

@@ -85,7 +85,7 @@ def test_group_packing_and_offsets(built):
     info = b.info()
     assert info["n_queries"] == 6
     # 100+40+900+40+800+40+50 = 1970 <= 2008 share a group; 9000 needs its own
-    # (a 16384-entry table); 20 cannot join it
+    # (a 16384-entry table in global memory); 20 cannot join it
     assert info["n_groups"] == 3
     seen = 0
     for g in range(info["n_groups"]):
