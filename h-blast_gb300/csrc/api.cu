@@ -89,7 +89,7 @@ static std::atomic<uint64_t> g_next_object_id{1};
 // size per launch, so a long query's large table does not cut the occupancy
 // of every other group in its batch.
 struct LaunchClass {
-    int mode;        // 0 chunk mode, 1 offset mode; + 2 when the tables have exact lengths
+    int mode;        // 0 chunk mode, 1 offset mode
     int smem_diag;   // per-warp 16-bit table entries (small for the global class)
     int first;       // groups [first, first + count) of the batch's group list
     int count;
@@ -208,20 +208,12 @@ int upload_batch(hbg_batch *b, int device) {
     CU(cudaMemcpy(b->d_pv, h.pv.data(), h.pv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_qcells, h.query_cells.data(), h.query_cells.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     {
-        // launch classes: (mode, table size bucket); tables of <= 2048 entries
-        // share one class (they all allow four CTAs per SM); larger shared
-        // tables (exact lengths, up to 4096) are bucketed and each class
-        // allocates its longest member; global-table groups form their own
-        // class per mode
-        static const int kBuckets[] = {2560, 3072, 4096};   // shared tables end at kSmemDiagMax
+        // launch classes: (mode, table size); shared tables (<= 2048 entries)
+        // share one class per mode, global-table groups form their own
         std::vector<std::pair<std::pair<int, int>, int32_t>> keyed;
         for (int32_t g = 0; g < (int32_t)h.groups.size(); ++g) {
             const HbgGroup &G = h.groups[g];
-            int size = 2048;
-            if (G.placement)
-                size = 64;
-            else if (G.diag_len > 2048)
-                size = *std::lower_bound(std::begin(kBuckets), std::end(kBuckets), G.diag_len);
+            const int size = G.placement ? 64 : std::max<int>(2048, G.diag_len);
             keyed.push_back({{G.mode, size}, g});
         }
         std::stable_sort(keyed.begin(), keyed.end(),
@@ -229,14 +221,9 @@ int upload_batch(hbg_batch *b, int device) {
         std::vector<int32_t> list;
         b->classes.clear();
         for (size_t i = 0; i < keyed.size(); ++i) {
-            const int size = keyed[i].first.second;
             if (i == 0 || keyed[i].first != keyed[i - 1].first)
-                b->classes.push_back(LaunchClass{keyed[i].first.first + (size > 2048 ? 2 : 0),
-                                                 size > 2048 ? 8 : size, (int)i, 0});
-            LaunchClass &lc = b->classes.back();
-            if (size > 2048)
-                lc.smem_diag = std::max(lc.smem_diag, h.groups[keyed[i].second].diag_len);
-            lc.count++;
+                b->classes.push_back(LaunchClass{keyed[i].first.first, keyed[i].first.second, (int)i, 0});
+            b->classes.back().count++;
             list.push_back(keyed[i].second);
         }
         if ((int)b->classes.size() > kMaxLaunchClasses)
@@ -1445,7 +1432,7 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
         return fail(HBG_ERR_TOO_LONG, "hbg_search_static: the batch needs " + std::to_string(need) +
                                           " scratch bytes, more than HBG_STATIC_SCRATCH_BYTES");
     if (global_diag_len(h, db) > 0)
-        return fail(HBG_ERR_TOO_LONG, "hbg_search_static: groups longer than 4056 letters or subjects "
+        return fail(HBG_ERR_TOO_LONG, "hbg_search_static: groups longer than 2008 letters or subjects "
                                       "longer than 32767 - window need global diagonal tables");
     DeviceScope ds(db->device);
     void *scratch = nullptr;

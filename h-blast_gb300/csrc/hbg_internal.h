@@ -24,8 +24,7 @@ struct HbgGroup {
     int64_t entry_base;   // first entry of this group in the batch entries array
     int64_t seq_base;     // first letter of this group in the batch letters array
     int32_t glen;         // letters in the group, gaps included
-    int32_t diag_len;     // table length >= glen + window: a power of two up to 2048 or for
-                          // global tables, else glen + window rounded up to 8
+    int32_t diag_len;     // power of two >= glen + window
     int32_t first_query;  // queries [first_query, first_query + n_queries)
     int32_t n_queries;
     int32_t placement;    // 0: diagonal table in shared memory, 1: global scratch

@@ -52,8 +52,7 @@ struct WordFinderArgs {
 // Shared memory the word-finder kernel needs for a CTA of `threads` threads.
 size_t wordfinder_smem_bytes(int threads, int smem_diag);
 cudaError_t wordfinder_configure();
-// mode: bit 0 = offset mode (else chunk mode), bit 1 = the groups' tables
-// have exact lengths (else powers of two)
+// mode: 0 chunk mode, 1 offset mode
 cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm);
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream);

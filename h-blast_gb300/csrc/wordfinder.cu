@@ -235,28 +235,13 @@ struct Item {
     int S;                   // subject length
     int j;                   // subject ordinal id
     Cell *diag;
-    int len;                 // table length L >= group length + window
-    int mask;                // L - 1 (used when L is a power of two)
+    int mask;                // table length - 1 (a power of two >= group length + window)
     int dofs;                // diagonal offset for this subject
     int window;
     const uint8_t *gseq;
     const int32_t *gctx;
     int first_query;
 };
-
-// Table index of diagonal q - s: q - s modulo L.  Tables of up to 2048
-// entries are powers of two (a mask); larger shared tables are sized exactly
-// (group length + window, rounded up to 8) to fit more warps per SM, and
-// take the remainder.  Any L >= group length + window keeps NCBI's results:
-// two diagonals of one subject that share an index differ by at least L, so
-// their hits are at least `window` apart.
-template <bool Exact, typename Cell>
-__device__ __forceinline__ int diag_index(const Item<Cell> &it, int q, int s_h) {
-    if (!Exact)
-        return (q - s_h) & it.mask;
-    const int t = (q - s_h) % it.len;
-    return t < 0 ? t + it.len : t;
-}
 
 // One hit on a diagonal whose cell holds `state` (NCBI's two-hit rule, with
 // the pending marker): returns the new cell value; when `on`, sets want_task
@@ -352,7 +337,7 @@ __device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d
 // them.  Queues hold 64: a replay batch starts only while at most 32 tasks
 // wait.  With drain, run everything and repeat until both lists are empty
 // (needed before the subject ends).  Warp-collective.
-template <bool Exact, typename Cell>
+template <typename Cell>
 __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
                       int &n_tasks, int &n_blk, int &blk_cur, bool drain) {
     using T = CellTraits<Cell>;
@@ -387,7 +372,7 @@ __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, W
                         a.hsps[o] = out;
                     }
                 }
-                const int d = diag_index<Exact>(it, q, s_h);
+                const int d = (q - s_h) & it.mask;
                 it.diag[d] = e.right ? (Cell)(T::kFlag | (uint32_t)(e.s_last_off - 2 + it.dofs))
                                      : (Cell)(s_h + it.dofs);
             }
@@ -416,7 +401,7 @@ __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, W
             if (act) {
                 s_h = wq.blk_s[src][i];
                 q = wq.blk_q[src][i];
-                d = diag_index<Exact>(it, q, s_h);
+                d = (q - s_h) & it.mask;
             }
             apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
         }
@@ -480,7 +465,7 @@ __device__ __forceinline__ void scan_words(const Item<Cell> &it, const Smem &sh,
 // Chunk mode, for sparse groups: one (group, subject) item scanned 32
 // offsets at a time, the hits of the chunk compacted in CPU order and applied
 // 32 at a time.  Warp-collective.
-template <bool Exact, typename Cell>
+template <typename Cell>
 __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
                                            WarpQueue &wq, const uint32_t *cs, const uint16_t *ents,
                                            int diag_alloc) {
@@ -494,8 +479,6 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     uint32_t c_next = 0, base_next = 0;
     if (it.S >= 3)
         scan_words(it, sh, cs, 0, &c_next, &base_next);
-    // exact tables: r0 = s0 mod L, so a hit's index needs no division
-    int r0 = 0;
     for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
         const uint32_t c = c_next, base = base_next;
         if (s0 + 32 <= it.S - 3)
@@ -534,27 +517,14 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
             const int s_h = s_n, q = q_n;
             if (hb + 32 < T_)
                 locate(hb + 32 + lane, &s_n, &q_n);
-            int d = 0;
-            if (Exact) {
-                // q - r0 - (s_h - s0) lies in (-L - 32, L): at most two wraps
-                d = q - r0 - (s_h - s0);
-                d += d < 0 ? it.len : 0;
-                d += d < 0 ? it.len : 0;
-            } else {
-                d = (q - s_h) & it.mask;
-            }
-            d = act ? d : 0;
+            const int d = act ? ((q - s_h) & it.mask) : 0;
             apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
             // queues hold 64: keep room for one more batch of 32
             while (n_tasks >= 32 || n_blk >= 32)
-                flush<Exact>(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
-        }
-        if (Exact) {
-            r0 += 32;
-            r0 -= r0 >= it.len ? it.len : 0;
+                flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
         }
     }
-    flush<Exact>(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
+    flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
     // advance the diagonal offset past this subject (NCBI Blast_ExtendWordExit)
     it.dofs += it.S + it.window;
     return item_hits;
@@ -567,7 +537,7 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
 // lie on distinct diagonals, so they need no ordering among themselves; the
 // next offset's first 32 entries are loaded while this one is applied.
 
-template <bool Exact, typename Cell>
+template <typename Cell>
 __device__ __forceinline__ void apply_offset(const Item<Cell> &it, bool act, int s_h, int q,
                                              WarpQueue &wq, int &n_tasks, int &n_blk, int blk_out) {
     using T = CellTraits<Cell>;
@@ -575,7 +545,7 @@ __device__ __forceinline__ void apply_offset(const Item<Cell> &it, bool act, int
     bool want_task = false, want_blk = false;
     int left = 0;
     if (act) {
-        const int d = diag_index<Exact>(it, q, s_h);
+        const int d = (q - s_h) & it.mask;
         const uint32_t cell = it.diag[d];
         const uint32_t next = two_hit_step<Cell>(cell, s_h, it.dofs, it.window, pend, true, want_task,
                                                  want_blk, left);
@@ -602,7 +572,7 @@ __device__ __forceinline__ void apply_offset(const Item<Cell> &it, bool act, int
     __syncwarp();
 }
 
-template <bool Exact, typename Cell>
+template <typename Cell>
 __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
                                                    WarpQueue &wq, const uint32_t *cs,
                                                    const uint16_t *ents, int diag_alloc) {
@@ -636,32 +606,29 @@ __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFin
                 q_next = (uint32_t)lane < nc ? __ldg(ents + nb + lane) : 0;
             }
             const int s_h = s0 + p;
-            apply_offset<Exact>(it, (uint32_t)lane < cc, s_h, q_cur, wq, n_tasks, n_blk, blk_cur);
+            apply_offset(it, (uint32_t)lane < cc, s_h, q_cur, wq, n_tasks, n_blk, blk_cur);
             while (n_tasks >= 32 || n_blk >= 32)
-                flush<Exact>(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
+                flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
             for (uint32_t e0 = 32; e0 < cc; e0 += 32) {
                 const bool act = e0 + lane < cc;
                 const int q = act ? __ldg(ents + cb + e0 + lane) : 0;
-                apply_offset<Exact>(it, act, s_h, q, wq, n_tasks, n_blk, blk_cur);
+                apply_offset(it, act, s_h, q, wq, n_tasks, n_blk, blk_cur);
                 while (n_tasks >= 32 || n_blk >= 32)
-                    flush<Exact>(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
+                    flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
             }
         }
     }
-    flush<Exact>(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
+    flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
     it.dofs += it.S + it.window;
     return item_hits;
 }
 
 }  // namespace
 
-// Mode bit 0: offset mode (else chunk mode); bit 1: exact-length tables (else
-// power-of-two tables).  Chunk mode is built for four 256-thread CTAs per SM
-// (64 registers a thread), offset mode (large tables) for one.
+// Mode 0 (chunk mode) is built for four 256-thread CTAs per SM (64 registers
+// a thread), mode 1 (offset mode, large tables) for one.
 template <int Mode>
-__global__ void __launch_bounds__(256, (Mode & 1) == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
-    constexpr bool kOffsets = (Mode & 1) != 0;
-    constexpr bool kExact = (Mode & 2) != 0;
+__global__ void __launch_bounds__(256, Mode == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sh = *reinterpret_cast<Smem *>(smem_raw);
     const int lane = threadIdx.x & 31;
@@ -725,16 +692,16 @@ __global__ void __launch_bounds__(256, (Mode & 1) == 0 ? 4 : 1) wordfinder_kerne
             // shared 16-bit table when the group fits it and window + S fits 15 bits;
             // otherwise this warp's 32-bit slice of the global scratch
             if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
-                Item<uint16_t> it{sp, S, j, diag_s, G.diag_len, G.diag_len - 1, dofs_s, window,
+                Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = kOffsets ? process_item_offsets<kExact>(it, a, sh, wq, cs, ents, a.smem_diag)
-                                : process_item<kExact>(it, a, sh, wq, cs, ents, a.smem_diag);
+                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
+                            : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
                 dofs_s = it.dofs;
             } else {
-                Item<uint32_t> it{sp, S, j, diag_g, G.diag_len, G.diag_len - 1, dofs_g, window,
+                Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = kOffsets ? process_item_offsets<kExact>(it, a, sh, wq, cs, ents, a.gdiag_len)
-                                : process_item<kExact>(it, a, sh, wq, cs, ents, a.gdiag_len);
+                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
+                            : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
                 dofs_g = it.dofs;
             }
             if (lane == 0)
@@ -761,35 +728,25 @@ cudaError_t wordfinder_configure() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const void *k[4] = {(const void *)wordfinder_kernel<0>, (const void *)wordfinder_kernel<1>,
-                        (const void *)wordfinder_kernel<2>, (const void *)wordfinder_kernel<3>};
-    for (const void *f : k) {
-        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        if (e != cudaSuccess)
-            return e;
-    }
-    return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(wordfinder_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(wordfinder_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
 }
 
 cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm) {
     const size_t smem = wordfinder_smem_bytes(threads, smem_diag);
-    switch (mode & 3) {
-    case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
-    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem);
-    case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<2>, threads, smem);
-    default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<3>, threads, smem);
-    }
+    return mode ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
 }
 
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream) {
     const size_t smem = wordfinder_smem_bytes(threads, a.smem_diag);
-    switch (mode & 3) {
-    case 0: wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a); break;
-    case 1: wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a); break;
-    case 2: wordfinder_kernel<2><<<blocks, threads, smem, stream>>>(a); break;
-    default: wordfinder_kernel<3><<<blocks, threads, smem, stream>>>(a); break;
-    }
+    if (mode)
+        wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a);
+    else
+        wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -36,8 +36,8 @@ class Choice:
 
 
 DEFAULT_CANDIDATES = (
-    Choice(1, 0, 256), Choice(1000, 0, 256), Choice(2008, 0, 256), Choice(2008, 0, 128),
-    Choice(4056, 0, 128), Choice(8152, 1, 256), Choice(16344, 1, 128),
+    Choice(1, 0, 256), Choice(1000, 0, 256), Choice(2008, 0, 256), Choice(4056, 0, 256),
+    Choice(6000, 0, 256), Choice(8152, 1, 256), Choice(16344, 1, 128),
 )
 STAGE2 = (dict(tile_subjects=32), dict(tile_subjects=128), dict(tile_subjects=512), dict(global_tables=True))
 

@@ -234,14 +234,7 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
         }
         G.n_queries = k - G.first_query;
         G.glen = glen;
-        // tables of up to 2048 entries are powers of two (index by mask);
-        // larger shared tables have the exact length, rounded up to 8, so
-        // more warps fit per SM; global tables stay powers of two
-        const int32_t need = glen + window;
-        if (next_pow2(need) <= 2048 || need > kSmemDiagMax)
-            G.diag_len = next_pow2(need);
-        else
-            G.diag_len = (need + 7) & ~7;
+        G.diag_len = next_pow2(glen + window);
         G.placement = G.diag_len <= kSmemDiagMax ? 0 : 1;
         if (G.placement)
             b.max_diag_len = std::max(b.max_diag_len, G.diag_len);

@@ -14,15 +14,17 @@
 namespace hbg {
 
 // Shared-memory diagonal tables (16-bit cells) hold at most this many
-// entries per warp; groups whose table is longer use the global scratch.
-// Measured on GB300: up to ~4096 entries shared tables are as fast or
-// faster; beyond, their footprint cuts resident warps to 8-12 per SM and
-// 32-bit tables in global memory (L2-resident, 32 warps per SM) are 17-23 %
-// faster (groups of 5000 to 15000 letters, and six-frame BLASTX queries).
-constexpr int32_t kSmemDiagMax = 4096;
-// Default group length: the table of a full group is 2048 entries (4 KB), small
-// enough for four 8-warp CTAs per SM.
-constexpr int32_t kDefaultGroupTable = 2048;
+// entries per warp; groups whose table is longer use 32-bit tables in the
+// global scratch.  Measured on GB300: 2048-entry tables are faster in shared
+// memory (four 8-warp CTAs per SM fit); longer shared tables cut resident
+// warps to 8-20 per SM, and L2-resident global tables with 32 warps per SM
+// beat them by 13-23 % (4096 to 32768 entries, BLASTP and six-frame BLASTX).
+constexpr int32_t kSmemDiagMax = 2048;
+// Default group length: a full group's table is 4096 entries (global memory).
+// On the 64-query batched workload 4056-letter groups (16 scans of the
+// database) measured 4 % faster than 2008-letter groups in shared memory (37
+// scans), and 6000-letter groups 2 % slower.
+constexpr int32_t kDefaultGroupTable = 4096;
 // Groups whose expected hits per subject offset reach this use offset mode
 // (off by default: chunk mode at high occupancy measured faster; the autotuner
 // and hbg_batch_set_mode choose offset mode explicitly).

@@ -396,7 +396,7 @@ int hbg_server_destroy(hbg_server *s);
  * stream; the call returns at once.
  *
  * Limits: batches whose scratch would exceed HBG_STATIC_SCRATCH_BYTES, groups
- * longer than 4056 letters and subjects longer than 32767 - window (both need
+ * longer than 2008 letters and subjects longer than 32767 - window (both need
  * global diagonal tables) are rejected with HBG_ERR_TOO_LONG.
  *
  * The first call on a device looks up the array's device address

@@ -76,8 +76,8 @@ def test_alone_equals_in_the_mix(small_db):
 
 @pytest.mark.parametrize("qlen", [3000, 9000, 20000])
 def test_long_query_tables(built, qlen):
-    # 3000: an exact-length shared table (3040 entries, indexed by remainder);
-    # 9000 and 20000: 16384- and 32768-entry tables in the global scratch
+    # 3000, 9000, 20000: 4096-, 16384- and 32768-entry tables in the global
+    # scratch (the 200-letter query's group uses a shared table)
     rng = np.random.default_rng(12)
     q = synth.random_letters(rng, qlen)
     db = synth.make_db(rng, 300, 300, 0.6, 30, 5000, 40, [q], lambda r: r.integers(100, 400), 0.5)

@@ -31,7 +31,9 @@ def test_search_static_matches_search(built):
     qs = [synth.random_letters(rng, n) for n in (300, 57, 1200, 800)]
     db = synth.make_db(rng, 3000, 300, 0.6, 30, 5000, 0.05, qs, 150, 0.5)
     gdb = hblast.Database(db.residues, db.offsets)
-    batch = hblast.Batch.proteins([hblast.ProteinQuery.blastp(q) for q in qs])
+    # groups of up to 2008 letters keep their diagonal tables in shared memory,
+    # which is what the static entry point can serve
+    batch = hblast.Batch.proteins([hblast.ProteinQuery.blastp(q) for q in qs], max_group_len=2008)
     ref = hblast.search(gdb, batch)          # the set-up search also makes the batch resident
     n, nq = len(ref.hsps), len(qs)
     assert n > 0
