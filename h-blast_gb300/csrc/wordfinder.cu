@@ -646,7 +646,11 @@ __global__ void __launch_bounds__(256, Mode == 0 ? 4 : 1) wordfinder_kernel(Word
         diag_s[i] = 0;
     const int window = a.window;
     // the 16-bit shared table starts past its limit so the first item clears it
+    // offsets of the three tables a warp may use: its shared 16-bit table,
+    // and its global slice seen as 16-bit or as 32-bit cells (switching views
+    // forces the other view to clear before its next use)
     int32_t dofs_s = CellTraits<uint16_t>::kLimit + 1, dofs_g = window;
+    int32_t dofs_h = CellTraits<uint16_t>::kLimit + 1;
     int cur_group = -1;
 
     for (;;) {
@@ -689,20 +693,30 @@ __global__ void __launch_bounds__(256, Mode == 0 ? 4 : 1) wordfinder_kernel(Word
             const int S = a.db_len[j];
             const uint8_t *sp = a.db + a.db_off[j];
             unsigned long long hits;
-            // shared 16-bit table when the group fits it and window + S fits 15 bits;
-            // otherwise this warp's 32-bit slice of the global scratch
+            // 16-bit cells when window + S fits 15 bits: in shared memory when the
+            // group's table fits there, else in this warp's slice of the global
+            // scratch (half the footprint of 32-bit cells, so the tables of all
+            // resident warps stay in L2); otherwise 32-bit cells in that slice
             if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
                 hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
                             : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
                 dofs_s = it.dofs;
+            } else if (window + S <= CellTraits<uint16_t>::kLimit) {
+                Item<uint16_t> it{sp, S, j, reinterpret_cast<uint16_t *>(diag_g), G.diag_len - 1, dofs_h,
+                                  window, a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
+                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, 2 * a.gdiag_len)
+                            : process_item(it, a, sh, wq, cs, ents, 2 * a.gdiag_len);
+                dofs_h = it.dofs;
+                dofs_g = kWrap32;                  // the 32-bit view clears before its next use
             } else {
                 Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
                 hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
                             : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
                 dofs_g = it.dofs;
+                dofs_h = CellTraits<uint16_t>::kLimit + 1;   // the 16-bit view clears before its next use
             }
             if (lane == 0)
                 atomicAdd(&sh.hits, hits);
