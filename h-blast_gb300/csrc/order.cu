@@ -164,21 +164,35 @@ __global__ void gather_hsps(const hbg_hsp *in, const uint32_t *vals,
 
 // Per-query ranges of the ordered list (sorted by query, then subject):
 // first[q] and end[q] bound query q's HSPs, passed[q] counts its subjects
-// with at least one HSP.  All three start at zero.
+// with at least one HSP.  All three start at zero.  Whole warps step
+// together (warp-uniform loop) so the subject counts can be summed per warp
+// and query before the atomic: the list is sorted, so a warp's lanes mostly
+// share one query.
 __global__ void query_ranges(const hbg_hsp *sorted, const unsigned long long *count, int64_t cap,
                              unsigned long long *first, unsigned long long *end,
                              unsigned long long *passed) {
     const int64_t n = live_count(count, cap);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t q = sorted[i].query, s = sorted[i].subject;
-        const bool new_q = i == 0 || sorted[i - 1].query != q;
-        if (new_q)
-            first[q] = (unsigned long long)i;
-        if (i == n - 1 || sorted[i + 1].query != q)
-            end[q] = (unsigned long long)(i + 1);
-        if (new_q || sorted[i - 1].subject != s)
-            atomicAdd(passed + q, 1ull);
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x - lane); base < n; base += stride) {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        int32_t q = -1;
+        bool fresh = false;
+        if (valid) {
+            q = sorted[i].query;
+            const int32_t s = sorted[i].subject;
+            const bool new_q = i == 0 || sorted[i - 1].query != q;
+            if (new_q)
+                first[q] = (unsigned long long)i;
+            if (i == n - 1 || sorted[i + 1].query != q)
+                end[q] = (unsigned long long)(i + 1);
+            fresh = new_q || sorted[i - 1].subject != s;
+        }
+        const unsigned same = __match_any_sync(0xffffffffu, q);
+        const unsigned cnt = __popc(__ballot_sync(0xffffffffu, fresh) & same);
+        if (valid && cnt && lane == __ffs(same) - 1)
+            atomicAdd(passed + q, (unsigned long long)cnt);
     }
 }
 
