@@ -16,6 +16,9 @@
 #include <array>
 #include <atomic>
 #include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <thread>
 
 namespace hbg {
@@ -26,7 +29,9 @@ const int8_t kBlosum62[28 * 32] = {
 #include "../csrc/blosum62.inc"
 };
 
-// Neighbour words of every query word, computed once per distinct word.
+// Neighbour words of every query word, computed once per distinct word and
+// kept for the life of the process (one cache per threshold), so batches
+// built one after another -- a serving loop -- reuse the enumerations.
 class NeighbourCache {
   public:
     explicit NeighbourCache(int32_t threshold) : threshold_(threshold) {
@@ -40,20 +45,18 @@ class NeighbourCache {
         lists_.resize(HBG_NUM_CELLS);
     }
 
-    // Read-only once every word in use has been enumerated (prepare()), so
-    // several threads may call it.
-    const std::vector<uint16_t> &get(uint8_t a, uint8_t b, uint8_t c) {
-        int32_t key = (a << 10) | (b << 5) | c;
-        if (!done_[key]) {
-            enumerate(a, b, c, &lists_[key]);
-            done_[key] = 1;
-        }
-        return lists_[key];
+    // The neighbours of a word that prepare() has enumerated; read-only, so
+    // any number of threads may call it.
+    const std::vector<uint16_t> &get(uint8_t a, uint8_t b, uint8_t c) const {
+        return lists_[(a << 10) | (b << 5) | c];
     }
 
-    // Enumerate the neighbourhoods of the flagged words, in parallel.
+    // Enumerate the neighbourhoods of the flagged words not seen before, in
+    // parallel.  Builds running at the same time take turns here; a list,
+    // once written, never changes.
     template <typename ParallelFor>
     void prepare(const std::vector<uint8_t> &need, ParallelFor &&pfor) {
+        std::lock_guard<std::mutex> lock(mu_);
         std::vector<int32_t> keys;
         for (int32_t k = 0; k < HBG_NUM_CELLS; ++k)
             if (need[k] && !done_[k])
@@ -90,7 +93,18 @@ class NeighbourCache {
     std::array<int, HBG_ALPHABET> row_max_;
     std::vector<uint8_t> done_;
     std::vector<std::vector<uint16_t>> lists_;
+    std::mutex mu_;
 };
+
+NeighbourCache &neighbour_cache(int32_t threshold) {
+    static std::mutex mu;
+    static std::map<int32_t, std::unique_ptr<NeighbourCache>> caches;
+    std::lock_guard<std::mutex> lock(mu);
+    std::unique_ptr<NeighbourCache> &c = caches[threshold];
+    if (!c)
+        c.reset(new NeighbourCache(threshold));
+    return *c;
+}
 
 // Run body(i) for i in [0, n) on up to 16 host threads (items taken from a
 // shared counter).
@@ -244,7 +258,7 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
     }
 
     // --- lookup tables: count, then fill ---
-    NeighbourCache nb(threshold);
+    NeighbourCache &nb = neighbour_cache(threshold);
     b.cells.assign((size_t)n_groups * HBG_CELL_STRIDE, 0);
     b.pv.assign((size_t)n_groups * HBG_PV_WORDS, 0);
     b.query_cells.assign(qs.size() * (size_t)HBG_NUM_CELLS, 0);
