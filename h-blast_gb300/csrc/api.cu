@@ -89,7 +89,7 @@ static std::atomic<uint64_t> g_next_object_id{1};
 // size per launch, so a long query's large table does not cut the occupancy
 // of every other group in its batch.
 struct LaunchClass {
-    int mode;        // 0 chunk mode, 1 offset mode
+    int mode;        // 0 chunk mode, 1 offset mode; + 2 for groups with global tables
     int smem_diag;   // per-warp 16-bit table entries (small for the global class)
     int first;       // groups [first, first + count) of the batch's group list
     int count;
@@ -221,8 +221,10 @@ int upload_batch(hbg_batch *b, int device) {
         std::vector<int32_t> list;
         b->classes.clear();
         for (size_t i = 0; i < keyed.size(); ++i) {
+            const bool global = h.groups[keyed[i].second].placement != 0;
             if (i == 0 || keyed[i].first != keyed[i - 1].first)
-                b->classes.push_back(LaunchClass{keyed[i].first.first, keyed[i].first.second, (int)i, 0});
+                b->classes.push_back(LaunchClass{keyed[i].first.first + (global ? 2 : 0), keyed[i].first.second,
+                                                 (int)i, 0});
             b->classes.back().count++;
             list.push_back(keyed[i].second);
         }

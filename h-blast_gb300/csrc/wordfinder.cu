@@ -625,10 +625,14 @@ __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFin
 
 }  // namespace
 
-// Mode 0 (chunk mode) is built for four 256-thread CTAs per SM (64 registers
-// a thread), mode 1 (offset mode, large tables) for one.
+// Mode bit 0: offset mode (else chunk mode); bit 1: the launch's groups keep
+// their diagonal tables in global memory (same code; that instantiation asks
+// for a small shared-memory carve-out so the L1 cache holds more of the
+// tables).  Chunk mode is built for four 256-thread CTAs per SM (64
+// registers a thread), offset mode (large tables) for one.
 template <int Mode>
-__global__ void __launch_bounds__(256, Mode == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
+__global__ void __launch_bounds__(256, (Mode & 1) == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
+    constexpr bool kOffsets = (Mode & 1) != 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sh = *reinterpret_cast<Smem *>(smem_raw);
     const int lane = threadIdx.x & 31;
@@ -700,21 +704,21 @@ __global__ void __launch_bounds__(256, Mode == 0 ? 4 : 1) wordfinder_kernel(Word
             if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
-                            : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
+                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
+                                : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
                 dofs_s = it.dofs;
             } else if (window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, reinterpret_cast<uint16_t *>(diag_g), G.diag_len - 1, dofs_h,
                                   window, a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, 2 * a.gdiag_len)
-                            : process_item(it, a, sh, wq, cs, ents, 2 * a.gdiag_len);
+                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, 2 * a.gdiag_len)
+                                : process_item(it, a, sh, wq, cs, ents, 2 * a.gdiag_len);
                 dofs_h = it.dofs;
                 dofs_g = kWrap32;                  // the 32-bit view clears before its next use
             } else {
                 Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = Mode ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
-                            : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
+                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
+                                : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
                 dofs_g = it.dofs;
                 dofs_h = CellTraits<uint16_t>::kLimit + 1;   // the 16-bit view clears before its next use
             }
@@ -738,29 +742,45 @@ size_t wordfinder_smem_bytes(int threads, int smem_diag) {
 }
 
 cudaError_t wordfinder_configure() {
-    // opt in to the largest shared-memory carve-out; launches size their own
+    // opt in to the largest shared-memory carve-out; launches size their own.
+    // The global-table instantiations prefer a carve-out of ~40 % (four CTAs
+    // need about 88 KB), leaving the rest of the SM's 256 KB to the L1 cache
+    // that holds their diagonal tables (measured 4 % faster than the driver's
+    // default choice); a hint the driver may round up.
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaError_t e = cudaFuncSetAttribute(wordfinder_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    if (e != cudaSuccess)
-        return e;
-    return cudaFuncSetAttribute(wordfinder_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    const void *k[4] = {(const void *)wordfinder_kernel<0>, (const void *)wordfinder_kernel<1>,
+                        (const void *)wordfinder_kernel<2>, (const void *)wordfinder_kernel<3>};
+    for (int m = 0; m < 4; ++m) {
+        cudaError_t e = cudaFuncSetAttribute(k[m], cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (e == cudaSuccess && (m & 2))
+            e = cudaFuncSetAttribute(k[m], cudaFuncAttributePreferredSharedMemoryCarveout, 40);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm) {
     const size_t smem = wordfinder_smem_bytes(threads, smem_diag);
-    return mode ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem)
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
+    switch (mode & 3) {
+    case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
+    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem);
+    case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<2>, threads, smem);
+    default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<3>, threads, smem);
+    }
 }
 
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream) {
     const size_t smem = wordfinder_smem_bytes(threads, a.smem_diag);
-    if (mode)
-        wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a);
-    else
-        wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a);
+    switch (mode & 3) {
+    case 0: wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a); break;
+    case 1: wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a); break;
+    case 2: wordfinder_kernel<2><<<blocks, threads, smem, stream>>>(a); break;
+    default: wordfinder_kernel<3><<<blocks, threads, smem, stream>>>(a); break;
+    }
     return cudaGetLastError();
 }
 
