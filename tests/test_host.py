@@ -171,3 +171,29 @@ def test_no_device_fails_loudly(built):
     with pytest.raises(hblast.HblastError) as e:
         hblast.Database(np.ones(10, np.uint8), np.array([0, 10]))
     assert e.value.code == hblast.core.HBG_ERR_NO_DEVICE
+
+
+def test_tuning_calls_validate_before_upload(built):
+    """hbg_batch_tune / hbg_batch_set_mode: argument checks and the host-side
+    placement change (no device needed: batches upload at their first search)."""
+    rng = np.random.default_rng(7)
+    qs = [synth.random_letters(rng, n) for n in (300, 1500)]
+    b = hblast.Batch.proteins([hblast.ProteinQuery.blastp(x) for x in qs], max_group_len=2008)
+    for bad in ((5, 0), (5000, 0), (-1, 0), (0, 2)):
+        with pytest.raises(hblast.HblastError):
+            b.tune(*bad)
+    b.tune(64, True).tune(0, False)        # valid values; global tables stay chosen
+    with pytest.raises(hblast.HblastError):
+        b.set_mode(2)
+    b.set_mode(1).set_mode(0, 0)
+    b.close()
+
+
+def test_autotune_table_round_trip(tmp_path):
+    from hblast import autotune
+    rows = [autotune.BucketResult(0, 300, 2, autotune.Choice(4056, 0, 256, 32, True), [])]
+    autotune.save(rows, tmp_path / "t.json")
+    back = autotune.load(tmp_path / "t.json")
+    assert back[0].best == rows[0].best
+    assert autotune.choice_for(100, back) == rows[0].best
+    assert autotune.choice_for(5000, back) == autotune.Choice(0, 0, 256)
