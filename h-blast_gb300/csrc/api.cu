@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -47,18 +48,90 @@ int bits_for(int64_t v) {
     return b;
 }
 
+// Device allocations of batches and search results go through a small
+// per-device cache: blocks freed while idle are kept (up to kPoolBytes per
+// device, blocks of up to kPoolBlock) and handed out again for requests of
+// at least half their size, so repeated small searches do not pay for
+// cudaMalloc / cudaFree each time.  Large blocks (databases) are not kept.
+constexpr size_t kPoolBytes = (size_t)2 << 30;
+constexpr size_t kPoolBlock = (size_t)512 << 20;
+
+struct DevicePool {
+    std::mutex mu;
+    std::map<void *, size_t> size_of;                 // every live allocation
+    std::map<int, std::multimap<size_t, void *>> idle; // per device, by size
+    std::map<int, size_t> idle_bytes;
+};
+DevicePool &pool() {
+    static DevicePool *p = new DevicePool;   // never destroyed: frees may run at exit
+    return *p;
+}
+
 template <class T>
 cudaError_t dalloc(T **p, size_t n) {
     *p = nullptr;
     if (n == 0)
         n = 1;
-    return cudaMalloc((void **)p, n * sizeof(T));
+    const size_t bytes = n * sizeof(T);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevicePool &P = pool();
+    {
+        std::lock_guard<std::mutex> lock(P.mu);
+        auto &idle = P.idle[dev];
+        auto it = idle.lower_bound(bytes);
+        if (it != idle.end() && it->first <= 2 * bytes) {
+            *p = (T *)it->second;
+            P.idle_bytes[dev] -= it->first;
+            idle.erase(it);
+            return cudaSuccess;
+        }
+    }
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess)
+        return e;
+    std::lock_guard<std::mutex> lock(P.mu);
+    P.size_of[q] = bytes;
+    *p = (T *)q;
+    return cudaSuccess;
 }
 
+// Free now (cudaFree waits for the device).
 template <class T>
 void dfree(T *&p) {
-    if (p)
+    if (p) {
+        {
+            DevicePool &P = pool();
+            std::lock_guard<std::mutex> lock(P.mu);
+            P.size_of.erase((void *)p);
+        }
         cudaFree(p);
+    }
+    p = nullptr;
+}
+
+// Give back a block that no GPU work still uses (the caller has synchronised):
+// kept for reuse when it fits the cache, else freed.
+template <class T>
+void dfree_idle(T *&p) {
+    if (!p)
+        return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevicePool &P = pool();
+    bool keep = false;
+    {
+        std::lock_guard<std::mutex> lock(P.mu);
+        auto it = P.size_of.find((void *)p);
+        if (it != P.size_of.end() && it->second <= kPoolBlock && P.idle_bytes[dev] + it->second <= kPoolBytes) {
+            P.idle[dev].emplace(it->second, (void *)p);
+            P.idle_bytes[dev] += it->second;
+            keep = true;
+        }
+    }
+    if (!keep)
+        dfree(p);
     p = nullptr;
 }
 
@@ -287,14 +360,16 @@ void free_result_device(hbg_result *r) {
     if (r->graph_exec)
         cudaGraphExecDestroy(r->graph_exec);
     r->graph_exec = nullptr;
-    dfree(r->d_raw);
-    dfree(r->d_sorted);
-    dfree(r->d_counters);
-    dfree(r->d_tile);
-    dfree(r->d_gdiag);
-    dfree(r->d_keys);
-    dfree(r->d_vals);
-    dfree(r->d_hist);
+    if (r->launched && !r->synced)
+        cudaStreamSynchronize(r->stream);    // nothing of this search may still run
+    dfree_idle(r->d_raw);
+    dfree_idle(r->d_sorted);
+    dfree_idle(r->d_counters);
+    dfree_idle(r->d_tile);
+    dfree_idle(r->d_gdiag);
+    dfree_idle(r->d_keys);
+    dfree_idle(r->d_vals);
+    dfree_idle(r->d_hist);
     for (auto &e : r->ev)
         if (e) {
             cudaEventDestroy(e);
@@ -1085,16 +1160,19 @@ int hbg_batch_destroy(hbg_batch *b) {
         return fail(HBG_ERR_INVALID, "null batch");
     if (b->device >= 0) {
         DeviceScope ds(b->device);
-        dfree(b->d_groups);
-        dfree(b->d_ctx);
-        dfree(b->d_queries);
-        dfree(b->d_letters);
-        dfree(b->d_ctx_of);
-        dfree(b->d_cells);
-        dfree(b->d_entries);
-        dfree(b->d_pv);
-        dfree(b->d_qcells);
-        dfree(b->d_group_list);
+        // searches of this batch may run on any stream: wait for the device
+        // (as cudaFree would), then keep the buffers for reuse
+        cudaDeviceSynchronize();
+        dfree_idle(b->d_groups);
+        dfree_idle(b->d_ctx);
+        dfree_idle(b->d_queries);
+        dfree_idle(b->d_letters);
+        dfree_idle(b->d_ctx_of);
+        dfree_idle(b->d_cells);
+        dfree_idle(b->d_entries);
+        dfree_idle(b->d_pv);
+        dfree_idle(b->d_qcells);
+        dfree_idle(b->d_group_list);
     }
     delete b;
     return HBG_OK;
@@ -1206,6 +1284,7 @@ int hbg_search(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, int64_t
         rc = launch_search(r);
     if (rc != HBG_OK) {
         if (!*out) {
+            cudaStreamSynchronize(r->stream);   // a partly enqueued search may still run
             free_result_device(r);
             delete r;
         }
