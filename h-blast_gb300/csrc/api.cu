@@ -321,6 +321,17 @@ int32_t global_diag_len(const hbg::HostBatch &h, const hbg_db *db) {
     return len;
 }
 
+// Subjects per work tile of one launch class: the batch's tuned value, else
+// up to 128, fewer when the class has too little work to give every CTA about
+// eight tiles (small databases and single queries would otherwise leave most
+// SMs idle).
+int32_t class_tile_subjects(const hbg_batch *b, const hbg_db *db, const LaunchClass &lc, int blocks) {
+    if (b->tile_subjects > 0)
+        return b->tile_subjects;
+    const int64_t want = (int64_t)db->n * lc.count / (8 * (int64_t)std::max(blocks, 1));
+    return (int32_t)std::max<int64_t>(8, std::min<int64_t>(128, want));
+}
+
 // CTA size and grid of each launch class: the CTA is halved until its
 // per-warp tables fit the shared-memory carve-out; the grid is one wave at
 // the occupancy that leaves (or the caller's num_blocksx).
@@ -481,12 +492,7 @@ int enqueue_search(hbg_result *r) {
     if (db->n > 0)   // the caller has run wordfinder_configure (not a stream operation)
         for (size_t c = 0; c < b->classes.size(); ++c) {
             const LaunchClass &lc = b->classes[c];
-            // tiles of up to 128 subjects, fewer when a class has too little
-            // work to give every CTA about eight tiles (small databases and
-            // single queries would otherwise leave most SMs idle)
-            const int64_t want = (int64_t)db->n * lc.count / (8 * (int64_t)r->shapes[c].blocks);
-            a.tile_subjects = b->tile_subjects > 0 ? b->tile_subjects
-                                                   : (int32_t)std::max<int64_t>(8, std::min<int64_t>(128, want));
+            a.tile_subjects = class_tile_subjects(b, db, lc, r->shapes[c].blocks);
             a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
             a.group_list = b->d_group_list + lc.first;
             a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
@@ -1452,10 +1458,11 @@ int hbg_search_sync(hbg_db *db, hbg_batch *batch, const hbg_gpu_options *opt, hb
 // ---------------------------------------------------------------------------
 // Search without allocation.
 //
-// For callers that may not allocate device memory at search time -- code
-// running inside a CUDA graph capture, allocator-free real-time services, or
-// hosts that hand the library a fixed memory budget up front -- this entry
-// point launches the word finder with its scratch in a file-scope device
+// For callers that may not allocate device memory at search time --
+// allocator-free real-time services whose latency budget has no room for
+// cudaMalloc's implicit synchronisation, and hosts that hand the library a
+// fixed memory budget at start-up and own every device byte after that -- this
+// entry point launches the word finder with its scratch in a file-scope device
 // array instead of cudaMalloc'd buffers.  The array is HBG_STATIC_SCRATCH_BYTES
 // on every device that loads the library and stays allocated until exit.
 
@@ -1508,6 +1515,8 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     const int64_t nq = (int64_t)h.queries.size(), ng = (int64_t)h.groups.size();
     // scratch layout: [tile counters (one per launch class) | per-query extensions |
     //                  per-query kept | per-group hits]
+    static_assert(kMaxLaunchClasses * sizeof(unsigned int) <= 256,
+                  "the tile counters must fit the 256-byte head of the static scratch");
     const int64_t need = 256 + 8 * (2 * nq + ng);
     if (need > HBG_STATIC_SCRATCH_BYTES)
         return fail(HBG_ERR_TOO_LONG, "hbg_search_static: the batch needs " + std::to_string(need) +
@@ -1568,6 +1577,8 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     if (db->n > 0) {
         for (size_t c = 0; c < batch->classes.size(); ++c) {
             const LaunchClass &lc = batch->classes[c];
+            a.tile_subjects = class_tile_subjects(batch, db, lc, shapes[c].blocks);
+            a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
             a.group_list = batch->d_group_list + lc.first;
             a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
             a.tile_counter = tile + c;

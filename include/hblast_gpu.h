@@ -379,9 +379,10 @@ int hbg_server_destroy(hbg_server *s);
 /* Run the word finder without allocating anything.  No counterpart in the
  * reference: H-BLAST allocates its buffers on every call.
  *
- * For callers that cannot call cudaMalloc at search time -- code running
- * while a CUDA graph is being captured, allocator-free real-time services, or
- * hosts that give the library a fixed memory budget at start-up.  It calls no
+ * For callers that cannot call cudaMalloc at search time: allocator-free
+ * real-time services (cudaMalloc and cudaFree may synchronise the device and
+ * take unbounded time), and hosts that give the library a fixed memory budget
+ * at start-up and account for every device byte after that.  It calls no
  * cudaMalloc, cudaFree or allocating library routine; its scratch (a tile
  * counter and per-query / per-group counters, 256 + 8 x (2 x queries + groups)
  * bytes) lives in a static device array of HBG_STATIC_SCRATCH_BYTES.

@@ -512,6 +512,211 @@ int64_t orc_search(const orc_query *q, int32_t threshold, int32_t window,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Many queries in one call.                                                 */
+/* Work items are (query, block of subjects), taken in order by a pool of    */
+/* threads from a shared counter; each item starts a fresh diagonal table,   */
+/* which changes no result (the offset trick makes the table's state fresh   */
+/* for every subject, Blast_ExtendWordExit).  Every HSP is kept: there is no */
+/* caller-sized buffer to overflow and no search is repeated.                */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int32_t q, begin, end;
+    hsp_vec hsps;
+    int32_t *subj;
+    int64_t subj_cap;
+    int64_t counters[3];
+} many_item;
+
+struct orc_result {
+    int32_t nq;
+    int64_t n_items;
+    int64_t *item_first;     /* per query: first item; items of a query are contiguous */
+    many_item *items;
+    const orc_query *qs;
+    const int32_t *const *cell_starts;
+    const int32_t *const *entries;
+    int32_t window;
+    const uint8_t *db;
+    const int64_t *db_off;
+    const int32_t *db_len;
+    int64_t next;            /* next item to take */
+    pthread_mutex_t lock;
+    int status;
+};
+
+static int run_item(orc_result *r, many_item *it)
+{
+    const orc_query *q = &r->qs[it->q];
+    diag_table dg;
+    if (diag_init(&dg, q->len, r->window))
+        return -1;
+    int rc = 0;
+    for (int32_t j = it->begin; j < it->end && rc == 0; ++j) {
+        int64_t before = it->hsps.n;
+        rc = word_finder_subject(q, r->cell_starts[it->q], r->entries[it->q], &dg,
+                                 r->db + r->db_off[j], r->db_len[j], &it->hsps, it->counters);
+        if (rc == 0 && it->hsps.n > before) {
+            if (it->hsps.n > it->subj_cap) {
+                int32_t *ns = (int32_t *)realloc(it->subj, (size_t)it->hsps.cap * sizeof(int32_t));
+                if (!ns) {
+                    rc = -1;
+                    break;
+                }
+                it->subj = ns;
+                it->subj_cap = it->hsps.cap;
+            }
+            for (int64_t k = before; k < it->hsps.n; ++k)
+                it->subj[k] = j;
+        }
+    }
+    free(dg.cell);
+    return rc;
+}
+
+static void *many_worker(void *arg)
+{
+    orc_result *r = (orc_result *)arg;
+    for (;;) {
+        pthread_mutex_lock(&r->lock);
+        int64_t i = r->next++;
+        pthread_mutex_unlock(&r->lock);
+        if (i >= r->n_items)
+            break;
+        if (run_item(r, &r->items[i])) {
+            pthread_mutex_lock(&r->lock);
+            r->status = -1;
+            pthread_mutex_unlock(&r->lock);
+        }
+    }
+    return NULL;
+}
+
+void orc_result_free(orc_result *r)
+{
+    if (!r)
+        return;
+    for (int64_t i = 0; i < r->n_items; ++i) {
+        free(r->items[i].hsps.v);
+        free(r->items[i].subj);
+    }
+    free(r->items);
+    free(r->item_first);
+    pthread_mutex_destroy(&r->lock);
+    free(r);
+}
+
+orc_result *orc_search_many(const orc_query *qs, int32_t nq, const int32_t *const *cell_starts,
+                            const int32_t *const *entries, int32_t window, const uint8_t *db,
+                            const int64_t *db_off, const int32_t *db_len, int32_t subj_begin,
+                            int32_t subj_end, int32_t nthreads, int64_t block_residues)
+{
+    if (!qs || nq < 0 || !cell_starts || !entries || window <= 0 || subj_end < subj_begin)
+        return NULL;
+    if (block_residues <= 0)
+        block_residues = 1 << 18;
+    orc_result *r = (orc_result *)calloc(1, sizeof(orc_result));
+    if (!r)
+        return NULL;
+    pthread_mutex_init(&r->lock, NULL);
+    r->nq = nq;
+    r->qs = qs;
+    r->cell_starts = cell_starts;
+    r->entries = entries;
+    r->window = window;
+    r->db = db;
+    r->db_off = db_off;
+    r->db_len = db_len;
+    /* subject blocks of about block_residues letters */
+    int64_t n_blocks = 0;
+    int32_t *bstart = (int32_t *)malloc(sizeof(int32_t) * ((size_t)(subj_end - subj_begin) + 2));
+    r->item_first = (int64_t *)calloc((size_t)nq + 1, sizeof(int64_t));
+    if (!bstart || !r->item_first) {
+        free(bstart);
+        orc_result_free(r);
+        return NULL;
+    }
+    for (int32_t j = subj_begin; j < subj_end;) {
+        bstart[n_blocks++] = j;
+        int64_t acc = 0;
+        while (j < subj_end && (acc == 0 || acc + db_len[j] <= block_residues))
+            acc += db_len[j++] + 1;
+    }
+    bstart[n_blocks] = subj_end;
+    r->n_items = n_blocks * nq;
+    r->items = (many_item *)calloc((size_t)(r->n_items > 0 ? r->n_items : 1), sizeof(many_item));
+    if (!r->items) {
+        free(bstart);
+        orc_result_free(r);
+        return NULL;
+    }
+    for (int32_t q = 0; q < nq; ++q) {
+        r->item_first[q] = (int64_t)q * n_blocks;
+        for (int64_t b = 0; b < n_blocks; ++b) {
+            many_item *it = &r->items[(int64_t)q * n_blocks + b];
+            it->q = q;
+            it->begin = bstart[b];
+            it->end = bstart[b + 1];
+        }
+    }
+    r->item_first[nq] = r->n_items;
+    free(bstart);
+    if (nthreads < 1)
+        nthreads = 1;
+    if (nthreads > r->n_items)
+        nthreads = (int32_t)(r->n_items > 0 ? r->n_items : 1);
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!th) {
+        orc_result_free(r);
+        return NULL;
+    }
+    int started = 0;
+    for (int t = 0; t < nthreads; ++t)
+        if (pthread_create(&th[t], NULL, many_worker, r) == 0)
+            ++started;
+    if (started == 0)
+        many_worker(r);
+    for (int t = 0; t < started; ++t)
+        pthread_join(th[t], NULL);
+    free(th);
+    if (r->status) {
+        orc_result_free(r);
+        return NULL;
+    }
+    return r;
+}
+
+int64_t orc_result_count(const orc_result *r, int32_t q)
+{
+    if (!r || q < 0 || q >= r->nq)
+        return -1;
+    int64_t n = 0;
+    for (int64_t i = r->item_first[q]; i < r->item_first[q + 1]; ++i)
+        n += r->items[i].hsps.n;
+    return n;
+}
+
+int orc_result_copy(const orc_result *r, int32_t q, orc_hsp *out, int32_t *out_subject,
+                    int64_t *counters)
+{
+    if (!r || q < 0 || q >= r->nq)
+        return -1;
+    int64_t k = 0;
+    for (int64_t i = r->item_first[q]; i < r->item_first[q + 1]; ++i) {
+        const many_item *it = &r->items[i];
+        if (out)
+            memcpy(out + k, it->hsps.v, (size_t)it->hsps.n * sizeof(orc_hsp));
+        if (out_subject)
+            memcpy(out_subject + k, it->subj, (size_t)it->hsps.n * sizeof(int32_t));
+        k += it->hsps.n;
+        if (counters)
+            for (int c = 0; c < 3; ++c)
+                counters[c] += it->counters[c];
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Six-frame translation (standard genetic code, NCBI transl_table 1).       */
 /* NCBI concatenates the six frames of a blastx query as contexts 0..5 =
  * frames +1,+2,+3,-1,-2,-3 (H-BLAST bins them by context at

@@ -92,6 +92,25 @@ int64_t orc_search_lut(const orc_query *q, const int32_t *cell_start,
                        orc_hsp *out, int32_t *out_subject, int64_t out_cap,
                        int64_t *counters);
 
+/* Search nq queries (query k with its CSR table cell_starts[k], entries[k])
+ * against subjects [subj_begin, subj_end) with nthreads threads taking
+ * (query, block of about block_residues subject letters) items from a shared
+ * counter (block_residues <= 0: 262144).  Every HSP is kept in memory owned
+ * by the result; results equal orc_search_lut per query.  NULL on an invalid
+ * argument or an allocation failure. */
+typedef struct orc_result orc_result;
+orc_result *orc_search_many(const orc_query *qs, int32_t nq, const int32_t *const *cell_starts,
+                            const int32_t *const *entries, int32_t window, const uint8_t *db,
+                            const int64_t *db_off, const int32_t *db_len, int32_t subj_begin,
+                            int32_t subj_end, int32_t nthreads, int64_t block_residues);
+/* HSPs of query q (-1 for a bad q). */
+int64_t orc_result_count(const orc_result *r, int32_t q);
+/* Copy query q's HSPs (subject order, then the CPU word finder's order) and
+ * their subject indices; counters[0..2] += its lookup hits, extensions, kept. */
+int orc_result_copy(const orc_result *r, int32_t q, orc_hsp *out, int32_t *out_subject,
+                    int64_t *counters);
+void orc_result_free(orc_result *r);
+
 /* Standard-code six-frame translation of a nucleotide query (codes
  * A=0 C=1 G=2 T=3, anything else N) into NCBIstdaa contexts in NCBI frame
  * order +1,+2,+3,-1,-2,-3, concatenated with one sentinel between frames.

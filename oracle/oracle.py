@@ -73,6 +73,16 @@ def lib() -> C.CDLL:
         L.orc_search_lut.restype = C.c_int64
         L.orc_translate6.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_translate6.restype = C.c_int32
+        L.orc_search_many.argtypes = [C.POINTER(_OrcQuery), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                      C.c_int64]
+        L.orc_search_many.restype = C.c_void_p
+        L.orc_result_count.argtypes = [C.c_void_p, C.c_int32]
+        L.orc_result_count.restype = C.c_int64
+        L.orc_result_copy.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_result_copy.restype = C.c_int
+        L.orc_result_free.argtypes = [C.c_void_p]
+        L.orc_result_free.restype = None
         _lib = L
     return _lib
 
@@ -115,33 +125,44 @@ def lookup_table(q: Query, threshold: int = 11):
 def search(q: Query, residues: np.ndarray, offsets: np.ndarray, threshold: int = 11, window: int = 40,
            nthreads: int = 1, subj_range=None, lut=None):
     """Search one query; returns (hsps structured array, subject index array, counters[3])."""
+    return search_many([q], residues, offsets, threshold, window, nthreads, subj_range,
+                       None if lut is None else [lut])[0]
+
+
+def search_many(queries, residues: np.ndarray, offsets: np.ndarray, threshold: int = 11, window: int = 40,
+                nthreads: int = 1, subj_range=None, luts=None, block_residues: int = 0):
+    """Search several queries in one call: (query, subject block) work items over `nthreads`
+    threads.  Returns one (hsps, subject indices, counters[3]) tuple per query; every HSP is
+    returned from a single pass (no capacity retries)."""
     residues = np.ascontiguousarray(residues, dtype=np.uint8)
     offsets = np.ascontiguousarray(offsets, dtype=np.int64)
     lens = np.ascontiguousarray(np.diff(offsets), dtype=np.int32)
     n = len(lens)
     lo, hi = subj_range if subj_range is not None else (0, n)
-    cq = q.c()
-    counters = np.zeros(3, dtype=np.int64)
-    cap = 1 << 12
-    while True:
-        out = np.zeros(cap, dtype=HSP_DTYPE)
-        subj = np.zeros(cap, dtype=np.int32)
-        counters[:] = 0
-        if lut is None:
-            got = lib().orc_search(C.byref(cq), threshold, window, residues.ctypes.data, offsets.ctypes.data,
-                                   lens.ctypes.data, lo, hi, nthreads, out.ctypes.data, subj.ctypes.data, cap,
-                                   counters.ctypes.data)
-        else:
-            cs = np.ascontiguousarray(lut[0], dtype=np.int32)
-            en = np.ascontiguousarray(lut[1], dtype=np.int32)
-            got = lib().orc_search_lut(C.byref(cq), cs.ctypes.data, en.ctypes.data, window,
-                                       residues.ctypes.data, offsets.ctypes.data, lens.ctypes.data, lo, hi,
-                                       nthreads, out.ctypes.data, subj.ctypes.data, cap, counters.ctypes.data)
-        if got < 0:
-            raise RuntimeError("oracle search failed")
-        if got <= cap:
-            return out[:got], subj[:got], counters.copy()
-        cap = int(got)
+    nq = len(queries)
+    if luts is None:
+        luts = [lookup_table(q, threshold) for q in queries]
+    cs = [np.ascontiguousarray(l[0], dtype=np.int32) for l in luts]
+    en = [np.ascontiguousarray(l[1] if len(l[1]) else np.zeros(1, np.int32), dtype=np.int32) for l in luts]
+    cq = (_OrcQuery * max(nq, 1))(*[q.c() for q in queries])
+    csp = (C.c_void_p * max(nq, 1))(*[a.ctypes.data for a in cs])
+    enp = (C.c_void_p * max(nq, 1))(*[a.ctypes.data for a in en])
+    r = lib().orc_search_many(cq, nq, csp, enp, window, residues.ctypes.data, offsets.ctypes.data,
+                              lens.ctypes.data, lo, hi, nthreads, block_residues)
+    if not r:
+        raise RuntimeError("oracle search failed")
+    try:
+        out = []
+        for k in range(nq):
+            m = lib().orc_result_count(r, k)
+            h = np.zeros(m, dtype=HSP_DTYPE)
+            subj = np.zeros(m, dtype=np.int32)
+            counters = np.zeros(3, dtype=np.int64)
+            lib().orc_result_copy(r, k, h.ctypes.data, subj.ctypes.data, counters.ctypes.data)
+            out.append((h, subj, counters))
+        return out
+    finally:
+        lib().orc_result_free(r)
 
 
 def translate6(nt: np.ndarray):

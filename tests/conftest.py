@@ -13,9 +13,10 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu on a GB300)")
 
 
-@pytest.fixture(scope="session")
+@pytest.fixture(scope="session", autouse=True)
 def built():
-    """Build the CUDA library and the oracle once per session (no GPU needed)."""
+    """Build the CUDA library and the oracle once per session (no GPU needed;
+    nvcc cross-compiles), so that every test finds them in a fresh checkout."""
     import __graft_entry__ as g
     g.build()
     return True

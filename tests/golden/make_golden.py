@@ -1,8 +1,8 @@
 """Regenerate tests/golden/reference_tables.json from the H-BLAST tree.
 
-Run in a checkout that has the reference at $HBLAST_REFERENCE (default
-/root/reference); the GPU machine does not have it and only reads the committed
-JSON.  What is extracted, and from where (paths inside the reference):
+Run with HBLAST_REFERENCE set to the root of a checkout of the H-BLAST
+repository (the directory that holds h_blast_v1.1/); tests only read the
+committed JSON.  What is extracted, and from where (paths inside the reference):
   - the BLOSUM62 table over NCBIstdaa, h_blast_v1.1/H-BLAST/h_blast.c:42-71
   - word-index constants CHARSIZE and AA_HITS_PER_CELL,
     h_blast_kernel.cu:1-3 and h_blast_kernel.h:39
@@ -16,12 +16,15 @@ import os
 import re
 from pathlib import Path
 
-REF = Path(os.environ.get("HBLAST_REFERENCE", "/root/reference")) / "h_blast_v1.1"
-HB = REF / "H-BLAST"
 OUT = Path(__file__).resolve().parent / "reference_tables.json"
 
 
 def main() -> None:
+    root = os.environ.get("HBLAST_REFERENCE")
+    if not root:
+        raise SystemExit("set HBLAST_REFERENCE to the root of an H-BLAST checkout")
+    REF = Path(root) / "h_blast_v1.1"
+    HB = REF / "H-BLAST"
     src = (HB / "h_blast.c").read_text()
     body = src[src.index("Blosum62[28][32]"):]
     rows = re.findall(r"\{([-\d,\s]+)\}", body)[:28]

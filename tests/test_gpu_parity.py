@@ -47,7 +47,8 @@ def small_db(built):
 
 
 def test_plain_single_query(built):
-    qs, db = synth.plain_blastp(seed=0, n_subjects=2000)
+    # the plain configuration as a whole: 1 query of 300 aa vs 20,000 subjects, seed 0
+    qs, db = synth.plain_blastp(seed=0, n_subjects=20000)
     gdb = hblast.Database(db.residues, db.offsets)
     pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
     res = hblast.search(gdb, hblast.Batch.proteins(pqs))

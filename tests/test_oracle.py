@@ -156,3 +156,34 @@ def test_threads_do_not_change_results(built):
     b = oracle.search(oracle.Query.blastp(q), db.residues, db.offsets, nthreads=4)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
     assert len(a[0]) > 0
+
+
+def test_search_many_equals_per_query_search():
+    """The multi-query driver (work items of (query, subject block) over a
+    thread pool, fresh diagonal table per item) gives the per-query search's
+    HSPs and counters: the offset trick makes every subject start from a
+    fresh diagonal state, so how subjects are split does not matter."""
+    import ctypes as C
+    from hblast import synth
+    rng = np.random.default_rng(5)
+    qs = [synth.random_letters(rng, n) for n in (40, 300, 777)]
+    db = synth.make_db(rng, 400, 300, 0.6, 30, 5000, 0.05, qs, lambda r: r.integers(50, 301),
+                       lambda r: r.uniform(0.3, 0.6))
+    oq = [oracle.Query.blastp(q) for q in qs]
+    lens = np.diff(db.offsets).astype(np.int32)
+    many = oracle.search_many(oq, db.residues, db.offsets, nthreads=3, block_residues=5000)
+    for q, (h, subj, cnt) in zip(oq, many):
+        cs, en = oracle.lookup_table(q, 11)
+        cs = np.ascontiguousarray(cs, np.int32)
+        en = np.ascontiguousarray(en if len(en) else np.zeros(1, np.int32), np.int32)
+        cap = 1 << 16
+        out = np.zeros(cap, dtype=oracle.HSP_DTYPE)
+        osub = np.zeros(cap, dtype=np.int32)
+        c0 = np.zeros(3, np.int64)
+        cq = q.c()
+        n = oracle.lib().orc_search_lut(C.byref(cq), cs.ctypes.data, en.ctypes.data, 40, db.residues.ctypes.data,
+                                        db.offsets.ctypes.data, lens.ctypes.data, 0, db.n, 1, out.ctypes.data,
+                                        osub.ctypes.data, cap, c0.ctypes.data)
+        assert 0 < n < cap
+        assert np.array_equal(h, out[:n]) and np.array_equal(subj, osub[:n])
+        assert np.array_equal(cnt, c0)

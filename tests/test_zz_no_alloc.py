@@ -1,6 +1,7 @@
 """hbg_search_static: the word finder with its scratch in a static device array,
-for callers that cannot allocate device memory while they search (code running
-during a CUDA graph capture, allocator-free services, fixed memory budgets).
+for callers that cannot allocate device memory while they search (real-time
+services that cannot afford cudaMalloc's synchronisation, hosts whose device
+memory budget is fixed at start-up).
 
 Two calls in a row through the C ABI must give the same HSPs and counters as
 hbg_search, bit for bit (tolerance 0: integer work).  The entry point leaves
@@ -25,17 +26,35 @@ def call_static(gdb, batch, d_hsps, cap, d_counts, stream):
                                    cap, C.c_void_p(d_counts.data_ptr()), C.c_void_p(stream.cuda_stream))
 
 
-def test_search_static_matches_search(built):
-    import torch
-    rng = np.random.default_rng(31)
+def make_batch(kind, rng):
+    """(database, batch) for one parity case; every
+    group stays within 2008 letters so its diagonal tables live in shared
+    memory, which is what the static entry point can serve."""
+    if kind == "blastx":
+        prot = synth.random_letters(rng, 400)
+        db = synth.make_db(rng, 1500, 300, 0.6, 30, 5000, 30, [prot], 150, 0.6)
+        nts = synth.blastx_queries(9, db, n_queries=3)
+        nts = [nt[:900] for nt in nts]                 # six frames of <= 300 letters: one group each
+        xd = np.full((3, 6), 16, dtype=np.int32)
+        cu = np.full((3, 6), 41, dtype=np.int32)
+        cu[1] = [30, 35, 41, 41, 38, 33]
+        return db, hblast.Batch.blastx(nts, xd, cu, max_group_len=2008)
     qs = [synth.random_letters(rng, n) for n in (300, 57, 1200, 800)]
     db = synth.make_db(rng, 3000, 300, 0.6, 30, 5000, 0.05, qs, 150, 0.5)
-    gdb = hblast.Database(db.residues, db.offsets)
-    # groups of up to 2008 letters keep their diagonal tables in shared memory,
-    # which is what the static entry point can serve
     batch = hblast.Batch.proteins([hblast.ProteinQuery.blastp(q) for q in qs], max_group_len=2008)
+    if kind == "offset_mode":
+        batch.set_mode(1)                              # one subject offset at a time, lanes over its cell
+    return db, batch
+
+
+@pytest.mark.parametrize("kind", ["blastp", "blastx", "offset_mode"])
+def test_search_static_matches_search(built, kind):
+    import torch
+    rng = np.random.default_rng(31)
+    db, batch = make_batch(kind, rng)
+    gdb = hblast.Database(db.residues, db.offsets)
     ref = hblast.search(gdb, batch)          # the set-up search also makes the batch resident
-    n, nq = len(ref.hsps), len(qs)
+    n, nq = len(ref.hsps), batch.info()["n_queries"]
     assert n > 0
     cap = n + 16
     d_hsps = torch.zeros(cap * 9, dtype=torch.int32, device="cuda")      # 9 int32 fields per record
