@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true", help="skip the one-query-per-launch comparison")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--group-len", type=int, default=0, help="letters per query group (0 = library default)")
+    p.add_argument("--mode", type=int, default=-1, help="hit mode of every group (-1 = library default)")
     return p.parse_args()
 
 
@@ -415,14 +417,16 @@ def main():
         cu6 = np.full((1, 6), 41, np.int32)
         pqs = list(qs)
 
-        def batch_of(specs, max_group_len=0):
+        def batch_of(specs, max_group_len=args.group_len):
             n = len(specs)
-            return hblast.Batch.blastx(specs, np.repeat(xd6, n, 0), np.repeat(cu6, n, 0), max_group_len=max_group_len)
+            b = hblast.Batch.blastx(specs, np.repeat(xd6, n, 0), np.repeat(cu6, n, 0), max_group_len=max_group_len)
+            return b.set_mode(args.mode) if args.mode >= 0 else b
     else:
         pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
 
-        def batch_of(specs, max_group_len=0):
-            return hblast.Batch.proteins(specs, max_group_len=max_group_len)
+        def batch_of(specs, max_group_len=args.group_len):
+            b = hblast.Batch.proteins(specs, max_group_len=max_group_len)
+            return b.set_mode(args.mode) if args.mode >= 0 else b
     batch = batch_of(pqs)
     binfo = batch.info()
     stream = torch.cuda.Stream()
