@@ -1006,6 +1006,8 @@ __global__ void __launch_bounds__(256, (Mode & 4) ? 3 : ((Mode & 1) == 0 ? 4 : 1
         sh.matrix[i] = c_blosum[i];
     for (int i = lane; i < a.smem_diag; i += 32)
         diag_s[i] = 0;
+    if (kOwner)
+        ow.cnt[lane] = 0;   // owner_distribute keeps it zero between batches
     const int window = a.window;
     // the 16-bit shared table starts past its limit so the first item clears it
     // offsets of the three tables a warp may use: its shared 16-bit table,
