@@ -281,24 +281,23 @@ int upload_batch(hbg_batch *b, int device) {
     CU(cudaMemcpy(b->d_pv, h.pv.data(), h.pv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(b->d_qcells, h.query_cells.data(), h.query_cells.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     {
-        // launch classes: (kernel mode, table size); shared tables (<= 2048
-        // entries) share one class per mode, global-table groups form their
-        // own.  Owner mode needs a shared table; a group set to it whose
-        // table is global runs in chunk mode.
+        // launch classes: (mode, table size); shared tables (<= 2048 entries)
+        // share one class per mode, global-table groups form their own
         std::vector<std::pair<std::pair<int, int>, int32_t>> keyed;
         for (int32_t g = 0; g < (int32_t)h.groups.size(); ++g) {
             const HbgGroup &G = h.groups[g];
             const int size = G.placement ? 64 : std::max<int>(2048, G.diag_len);
-            const int kmode = G.placement ? 2 + (G.mode == 1 ? 1 : 0) : (G.mode == 2 ? 4 : G.mode);
-            keyed.push_back({{kmode, size}, g});
+            keyed.push_back({{G.mode, size}, g});
         }
         std::stable_sort(keyed.begin(), keyed.end(),
                          [](const auto &x, const auto &y) { return x.first < y.first; });
         std::vector<int32_t> list;
         b->classes.clear();
         for (size_t i = 0; i < keyed.size(); ++i) {
+            const bool global = h.groups[keyed[i].second].placement != 0;
             if (i == 0 || keyed[i].first != keyed[i - 1].first)
-                b->classes.push_back(LaunchClass{keyed[i].first.first, keyed[i].first.second, (int)i, 0});
+                b->classes.push_back(LaunchClass{keyed[i].first.first + (global ? 2 : 0), keyed[i].first.second,
+                                                 (int)i, 0});
             b->classes.back().count++;
             list.push_back(keyed[i].second);
         }
@@ -347,7 +346,7 @@ int plan_launches(const hbg_batch *b, const hbg_gpu_options &o, int device, std:
         // tables fill shared memory, and smaller CTAs pack it better
         int best_t = 0, best_per = 0, best_warps = -1;
         for (int t = o.num_threadsx; t >= 32; t = t > 64 ? ((t / 2) + 31) / 32 * 32 : 0) {
-            if (hbg::wordfinder_smem_bytes(lc.mode, t, lc.smem_diag) > (size_t)optin)
+            if (hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
                 continue;
             int per = 0;
             if (hbg::wordfinder_occupancy(lc.mode, t, lc.smem_diag, &per) != cudaSuccess || per < 1)
@@ -1129,7 +1128,7 @@ int hbg_batch_lookup_table(const hbg_batch *b, int32_t g, uint32_t *cells, uint1
 }
 
 int hbg_batch_set_mode(hbg_batch *b, int32_t g, int32_t mode) {
-    if (!b || mode < 0 || mode > 2 || g >= (int32_t)b->host.groups.size())
+    if (!b || (mode != 0 && mode != 1) || g >= (int32_t)b->host.groups.size())
         return fail(HBG_ERR_INVALID, "hbg_batch_set_mode: bad argument");
     if (b->device >= 0)
         return fail(HBG_ERR_STATE, "batch already uploaded: set modes before the first search");

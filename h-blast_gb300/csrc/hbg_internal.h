@@ -28,7 +28,7 @@ struct HbgGroup {
     int32_t first_query;  // queries [first_query, first_query + n_queries)
     int32_t n_queries;
     int32_t placement;    // 0: diagonal table in shared memory, 1: global scratch
-    int32_t mode;         // 0: chunk mode, 1: offset mode (dense hits), 2: owner mode (shared tables)
+    int32_t mode;         // 0: chunk mode (sparse hits), 1: offset mode (dense hits)
 };
 
 struct HbgContext {

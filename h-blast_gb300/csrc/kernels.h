@@ -50,11 +50,10 @@ struct WordFinderArgs {
 };
 
 // Shared memory the word-finder kernel needs for a CTA of `threads` threads.
-size_t wordfinder_smem_bytes(int mode, int threads, int smem_diag);
+size_t wordfinder_smem_bytes(int threads, int smem_diag);
 cudaError_t wordfinder_configure();
 // mode: bit 0 = offset mode (else chunk mode); bit 1 = the groups keep
-// their diagonal tables in global memory (kernel built to favour L1); bit 2 =
-// owner mode (lanes own diagonals; shared tables only; bits 0-1 clear)
+// their diagonal tables in global memory (kernel built to favour L1)
 cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm);
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream);

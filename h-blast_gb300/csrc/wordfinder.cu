@@ -217,8 +217,15 @@ constexpr int32_t kWrap32 = 1 << 29;
 // until the extension has written the diagonal's real state.
 
 constexpr int kQueue = 64;
+// Subject letters reach the scan through a per-warp ring in shared memory,
+// filled by 16-byte asynchronous copies (cp.async) two blocks ahead of the
+// scan.  The ring is small so that four 8-warp CTAs with 2048-entry tables
+// still fit an SM.
+constexpr int kStageBlock = 64;    // letters per block: 16 bytes for each of lanes 0..3
+constexpr int kStageRing = 4;      // blocks held: the scan's two, and two in flight
 
 struct WarpQueue {
+    uint4 stage[kStageRing * kStageBlock / 16];   // ring of subject letters
     int task_s[kQueue];      // subject offset of the second hit
     int task_q[kQueue];      // group-local query offset
     int task_left[kQueue];   // one past the first hit's word (subject offset)
@@ -429,32 +436,81 @@ __device__ __forceinline__ void restart_offset(Item<Cell> &it, int diag_alloc) {
     }
 }
 
-// Word index of offset s0+lane, presence test and cell bounds:
-// *c = hits of that offset, *base = first entry.  Warp-collective.
-template <typename Cell>
-__device__ __forceinline__ void scan_words(const Item<Cell> &it, const Smem &sh, const uint32_t *cs,
-                                           int s0, uint32_t *c, uint32_t *base) {
-    const int lane = threadIdx.x & 31;
-    // letters s0+lane, +1, +2: one coalesced load, two shuffles; the
-    // database has sentinels and tail padding, so reading past the
-    // subject end stays inside the allocation
-    const int sp = s0 + lane;
-    const uint32_t b0 = it.s[sp];
-    const uint32_t x = lane < 2 ? (uint32_t)it.s[s0 + 32 + lane] : 0u;
-    uint32_t b1 = __shfl_down_sync(0xffffffffu, b0, 1);
-    uint32_t b2 = __shfl_down_sync(0xffffffffu, b0, 2);
-    const uint32_t x0 = __shfl_sync(0xffffffffu, x, 0);
-    const uint32_t x1 = __shfl_sync(0xffffffffu, x, 1);
-    if (lane == 31) {
-        b1 = x0;
-        b2 = x1;
-    } else if (lane == 30) {
-        b2 = x0;
+// Subject letters staged for the scan: blocks of kStageBlock letters counted
+// from the 16-byte aligned address at or before the subject's first letter.
+// Block k goes to ring slot k % kStageRing.  `next` is the next block the scan
+// will need; blocks next and next + 1 have been issued.
+struct Stage {
+    int next;
+};
+
+constexpr int kStageLanes = kStageBlock / 16;
+
+// Issue block k: lanes 0..kStageLanes-1 copy 16 bytes each.  A segment is
+// copied only when it holds a letter of the subject (relative position <
+// delta + S); it then ends at most 15 bytes past the subject, inside the
+// database buffer (a sentinel after every subject, 64 bytes of tail padding).
+// Other segments are zero-filled without reading.  Every lane commits one
+// copy group per block (empty for lanes that copy nothing).
+__device__ __forceinline__ void stage_issue(WarpQueue &wq, const uint8_t *s, int S, int k, int lane) {
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(s);
+    const int delta = (int)(sa & 15);
+    const int r = k * kStageBlock + lane * 16;
+    if (lane < kStageLanes) {
+        const bool in = r < delta + S;
+        const uint8_t *src = reinterpret_cast<const uint8_t *>(sa & ~(uintptr_t)15) + (in ? r : 0);
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&wq.stage[(k & (kStageRing - 1)) * kStageLanes + lane]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(in ? 16 : 0)
+                     : "memory");
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void stage_begin(Stage &st, WarpQueue &wq, const uint8_t *s, int S, int lane) {
+    stage_issue(wq, s, S, 0, lane);
+    stage_issue(wq, s, S, 1, lane);
+    st.next = 0;
+}
+
+// Make blocks up to `blk` resident: for each newly needed block b, wait for
+// its copy (all but the newest group, b + 1, complete), then issue b + 2 into
+// the slot of b - 2, which no chunk needs any more (a chunk reads at most
+// blocks b - 1 and b).  Warp-collective (blk is warp-uniform).
+__device__ __forceinline__ void stage_upto(Stage &st, WarpQueue &wq, const uint8_t *s, int S, int blk,
+                                           int lane) {
+    while (st.next <= blk) {
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncwarp();
+        stage_issue(wq, s, S, st.next + 2, lane);
+        st.next++;
+    }
+}
+
+// Before the warp leaves a subject: no copy may still write its ring.
+__device__ __forceinline__ void stage_end() {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncwarp();
+}
+
+// Word index of offset s0+lane (three letters from the staged ring),
+// presence test and cell bounds: *c = hits of that offset, *base = first
+// entry.  Warp-collective.
+template <typename Cell>
+__device__ __forceinline__ void scan_words(const Item<Cell> &it, Stage &stg, WarpQueue &wq, const Smem &sh,
+                                           const uint32_t *cs, int s0, uint32_t *c, uint32_t *base) {
+    const int lane = threadIdx.x & 31;
+    // the words of this chunk need letters up to delta + s0 + 33
+    const int delta = (int)(reinterpret_cast<uintptr_t>(it.s) & 15);
+    stage_upto(stg, wq, it.s, it.S, (delta + s0 + 33) / kStageBlock, lane);
+    const uint8_t *ring = reinterpret_cast<const uint8_t *>(wq.stage);
+    constexpr int kMask = kStageRing * kStageBlock - 1;
+    const int sp = s0 + lane;
+    const int r = delta + sp;
     *c = 0;
     *base = 0;
     if (sp <= it.S - 3) {
-        const uint32_t w = (b0 << 10) | (b1 << 5) | b2;
+        const uint32_t w = ((uint32_t)ring[r & kMask] << 10) | ((uint32_t)ring[(r + 1) & kMask] << 5) |
+                           (uint32_t)ring[(r + 2) & kMask];
         if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
             *base = __ldg(cs + w);
             *c = __ldg(cs + w + 1) - *base;
@@ -473,16 +529,18 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     restart_offset(it, diag_alloc);
     int n_tasks = 0, n_blk = 0, blk_cur = 0;
     unsigned long long item_hits = 0;
+    Stage stg;
+    stage_begin(stg, wq, it.s, it.S, lane);
     // software pipeline: the next chunk's cell bounds are loaded while this
     // chunk's hits are applied, and each batch's query offsets while the
     // previous batch is applied
     uint32_t c_next = 0, base_next = 0;
     if (it.S >= 3)
-        scan_words(it, sh, cs, 0, &c_next, &base_next);
+        scan_words(it, stg, wq, sh, cs, 0, &c_next, &base_next);
     for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
         const uint32_t c = c_next, base = base_next;
         if (s0 + 32 <= it.S - 3)
-            scan_words(it, sh, cs, s0 + 32, &c_next, &base_next);
+            scan_words(it, stg, wq, sh, cs, s0 + 32, &c_next, &base_next);
         uint32_t incl = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -525,6 +583,7 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
         }
     }
     flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
+    stage_end();
     // advance the diagonal offset past this subject (NCBI Blast_ExtendWordExit)
     it.dofs += it.S + it.window;
     return item_hits;
@@ -580,9 +639,11 @@ __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFin
     restart_offset(it, diag_alloc);
     int n_tasks = 0, n_blk = 0, blk_cur = 0;
     unsigned long long item_hits = 0;
+    Stage stg;
+    stage_begin(stg, wq, it.s, it.S, lane);
     for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
         uint32_t c, base;
-        scan_words(it, sh, cs, s0, &c, &base);
+        scan_words(it, stg, wq, sh, cs, s0, &c, &base);
         item_hits += __reduce_add_sync(0xffffffffu, c);
         unsigned m = __ballot_sync(0xffffffffu, c != 0);
         uint32_t nb = 0, nc = 0;
@@ -619,358 +680,7 @@ __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFin
         }
     }
     flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
-    it.dofs += it.S + it.window;
-    return item_hits;
-}
-
-// ---------------------------------------------------------------------------
-// Owner mode, for groups whose diagonal table fits shared memory.  Lane L owns
-// the diagonals d with (d & 31) == L and applies their hits itself, in CPU
-// order, from a ring FIFO in shared memory.  No other lane touches its
-// diagonals, so hits of one batch need no ordering among lanes (no match.any
-// chains), and the table is laid out so that the 32 lanes' cells fall in 32
-// distinct banks.  Hits are located in CPU order as in chunk mode, 32 at a
-// time, and handed to their owners (a batch's hits for one owner keep their
-// lane order); owners then apply them in rounds, one hit per lane per round.
-// A hit that meets a diagonal whose extension is queued is parked in its
-// owner's park list, in order, and replayed once the extension has written
-// the diagonal's state.  Subject letters reach the scan through a 1 KB
-// shared-memory ring filled with 16-byte vector loads one 512-letter block
-// ahead of the scan.
-
-constexpr int kFifo = 16;          // hits per lane in the ring FIFO (a power of two)
-constexpr int kPark = 6;           // parked hits per lane
-constexpr int kStageBlock = 512;   // letters per staged block: 16 per lane
-constexpr int kStageRing = 2;      // staged blocks held (the scan reads at most two at a time)
-
-struct OwnerWarp {
-    uint4 stage[kStageRing * kStageBlock / 16];   // ring of subject letters
-    uint32_t fifo[kFifo][32];                     // s << 16 | q; row = slot, column = owner lane
-    uint32_t park[kPark][32];
-    int task_s[kQueue];                           // queued extensions, oldest first
-    int task_q[kQueue];
-    int task_left[kQueue];
-    uint32_t cnt[32];                             // hits one batch hands to each owner lane
-};
-static_assert(sizeof(OwnerWarp) % 16 == 0, "per-warp regions keep 16-byte alignment");
-static_assert(sizeof(OwnerWarp) >= sizeof(WarpQueue),
-              "subjects too long for 16-bit cells reuse a warp's owner-mode memory as its chunk-mode queue");
-
-// Position of cell i in a warp's table: the cells of 32 consecutive
-// diagonals (one per owner lane) occupy 32 distinct 4-byte banks.
-__device__ __forceinline__ int swz(int i) { return ((i >> 6) << 6) | ((i & 31) << 1) | ((i >> 5) & 1); }
-
-struct OwnerState {
-    int head, tail;   // this lane's FIFO: entries [head, tail) (positions mod kFifo)
-    int np;           // this lane's parked hits
-    bool stall;       // no FIFO rounds for this lane until a flush (park list full)
-    int n_tasks;      // queued extensions (warp-uniform)
-};
-
-// Subject letters staged for the scan.
-struct Stage {
-    const uint4 *org;   // 16-byte aligned, at or before the subject's first letter
-    int delta;          // first letter's distance from org
-    int end;            // delta + subject length
-    int next;           // next block to store in the ring
-    uint4 v;            // that block's 16 bytes for this lane (loaded ahead)
-};
-
-// Block k's 16 bytes for this lane.  A 16-byte segment is read only when it
-// holds a letter of the subject (relative position < end); it then ends at
-// most 15 bytes past the subject, inside the database buffer (one sentinel
-// after every subject, 64 bytes of tail padding).
-__device__ __forceinline__ uint4 stage_load(const Stage &st, int k, int lane) {
-    const int r = k * kStageBlock + lane * 16;
-    return r < st.end ? __ldg(st.org + (size_t)k * (kStageBlock / 16) + lane) : make_uint4(0, 0, 0, 0);
-}
-
-// Make staged blocks up to `blk` resident; each store issues the load of the
-// following block.  Warp-collective (blk is warp-uniform).
-__device__ __forceinline__ void stage_upto(Stage &st, OwnerWarp &ow, int blk, int lane) {
-    while (st.next <= blk) {
-        ow.stage[(st.next & (kStageRing - 1)) * (kStageBlock / 16) + lane] = st.v;
-        st.next++;
-        st.v = stage_load(st, st.next, lane);
-        __syncwarp();
-    }
-}
-
-// scan_words over the staged letters.
-__device__ __forceinline__ void scan_words_staged(const Item<uint16_t> &it, Stage &stg, OwnerWarp &ow,
-                                                  const Smem &sh, const uint32_t *cs, int s0, uint32_t *c,
-                                                  uint32_t *base) {
-    const int lane = threadIdx.x & 31;
-    stage_upto(stg, ow, (stg.delta + s0 + 33) / kStageBlock, lane);
-    const uint8_t *ring = reinterpret_cast<const uint8_t *>(ow.stage);
-    constexpr int kMask = kStageRing * kStageBlock - 1;
-    const int sp = s0 + lane;
-    const int r = stg.delta + sp;
-    *c = 0;
-    *base = 0;
-    if (sp <= it.S - 3) {
-        const uint32_t w = ((uint32_t)ring[r & kMask] << 10) | ((uint32_t)ring[(r + 1) & kMask] << 5) |
-                           (uint32_t)ring[(r + 2) & kMask];
-        if ((sh.pv[w >> 5] >> (w & 31)) & 1u) {
-            *base = __ldg(cs + w);
-            *c = __ldg(cs + w + 1) - *base;
-        }
-    }
-}
-
-// Append this lane's extension (if want) to the warp's queue.  Warp-collective.
-__device__ __forceinline__ void push_task(OwnerWarp &ow, int &n_tasks, bool want, int s_h, int q, int left) {
-    const unsigned tm = __ballot_sync(0xffffffffu, want);
-    if (want) {
-        const int p = n_tasks + __popc(tm & lanemask_lt());
-        ow.task_s[p] = s_h;
-        ow.task_q[p] = q;
-        ow.task_left[p] = left;
-    }
-    n_tasks += __popc(tm);
-    __syncwarp();
-}
-
-// Apply one hit to its diagonal: false if the diagonal's extension is still
-// queued (the hit must wait), else the two-hit step (want_task/left set when
-// it starts an extension).
-__device__ __forceinline__ bool owner_apply(const Item<uint16_t> &it, uint32_t pend, int s_h, int q,
-                                            bool &want_task, int &left) {
-    uint16_t *cell = it.diag + swz((q - s_h) & it.mask);
-    const uint32_t st = *cell;
-    if (st == pend)
-        return false;
-    bool wb = false;
-    const uint32_t nx = two_hit_step<uint16_t>(st, s_h, it.dofs, it.window, pend, true, want_task, wb, left);
-    if (nx != st)
-        *cell = (uint16_t)nx;
-    return true;
-}
-
-// Run queued extensions (the oldest 32, or all of them when draining or when
-// at most 32 wait), then replay parked hits in order; with drain, repeat until
-// nothing is queued or parked.  A replay pass stops while more than 32
-// extensions wait (the queue holds 64); its unreplayed hits stay parked behind
-// the re-parked ones, in order, and their lanes take no FIFO round until the
-// next pass finishes them.  Warp-collective.
-__device__ void owner_flush(const Item<uint16_t> &it, const WordFinderArgs &a, Smem &sh, OwnerWarp &ow,
-                            OwnerState &os, bool drain) {
-    using T = CellTraits<uint16_t>;
-    const int lane = threadIdx.x & 31;
-    const uint32_t pend = T::kFlag | (uint32_t)(it.dofs - 1);
-    bool again;
-    do {
-        const int run = (!drain && os.n_tasks > 32) ? 32 : os.n_tasks;
-        for (int t0 = 0; t0 < run; t0 += 32) {
-            const int i = t0 + lane;
-            if (i < run) {
-                const int s_h = ow.task_s[i], q = ow.task_q[i];
-                const int ci = __ldg(it.gctx + q);
-                const HbgContext C = a.contexts[ci];
-                const HbgQueryDesc Q = a.queries[C.query];
-                const int ql = q - Q.start;
-                const Ext e = extend_two_hit(sh.matrix, it.s, it.S, it.gseq + Q.start, Q.len, ow.task_left[i],
-                                             s_h, ql, C.x_dropoff);
-                atomicAdd(&sh.q_ext[C.query - it.first_query], 1u);
-                if (e.score >= C.cutoff) {
-                    atomicAdd(&sh.q_kept[C.query - it.first_query], 1u);
-                    const unsigned long long o = atomicAdd(a.hsp_count, 1ull);
-                    if ((long long)o < a.hsp_cap) {
-                        hbg_hsp out;
-                        out.query = C.query;
-                        out.subject = it.j;
-                        out.q_start = e.q_start;
-                        out.s_start = e.s_start;
-                        out.q_off = ql;
-                        out.s_off = s_h;
-                        out.len = e.len;
-                        out.score = e.score;
-                        out.context = C.local;
-                        a.hsps[o] = out;
-                    }
-                }
-                it.diag[swz((q - s_h) & it.mask)] =
-                    e.right ? (uint16_t)(T::kFlag | (uint32_t)(e.s_last_off - 2 + it.dofs)) : (uint16_t)(s_h + it.dofs);
-            }
-        }
-        __syncwarp();
-        if (run < os.n_tasks) {                 // at most 31 wait: move them to the front
-            const int rest = os.n_tasks - run;
-            int ts = 0, tq = 0, tl = 0;
-            if (lane < rest) {
-                ts = ow.task_s[run + lane];
-                tq = ow.task_q[run + lane];
-                tl = ow.task_left[run + lane];
-            }
-            __syncwarp();
-            if (lane < rest) {
-                ow.task_s[lane] = ts;
-                ow.task_q[lane] = tq;
-                ow.task_left[lane] = tl;
-            }
-            __syncwarp();
-        }
-        os.n_tasks -= run;
-        // replay this lane's parked hits in order
-        int w = 0, r = 0;
-        bool cut = false;
-        for (; __any_sync(0xffffffffu, r < os.np); ++r) {
-            if (os.n_tasks > 32) {
-                cut = true;
-                break;
-            }
-            bool want = false;
-            int left = 0, s_h = 0, q = 0;
-            if (r < os.np) {
-                const uint32_t e = ow.park[r][lane];
-                s_h = (int)(e >> 16);
-                q = (int)(e & 0xffffu);
-                if (!owner_apply(it, pend, s_h, q, want, left))
-                    ow.park[w++][lane] = e;
-            }
-            push_task(ow, os.n_tasks, want, s_h, q, left);
-        }
-        if (cut && r < os.np) {
-            for (int k = r; k < os.np; ++k)
-                ow.park[w + (k - r)][lane] = ow.park[k][lane];
-            os.np = w + (os.np - r);
-        } else {
-            os.np = w;
-        }
-        __syncwarp();
-        os.stall = cut ? os.np > 0 : os.np >= kPark;
-        again = drain ? (os.n_tasks > 0 || __any_sync(0xffffffffu, os.np > 0)) : (os.n_tasks >= 32 || cut);
-    } while (again);
-}
-
-// One round: every lane with a queued hit (and room to park one) applies or
-// parks its oldest.  Warp-collective.
-__device__ __forceinline__ void owner_round(const Item<uint16_t> &it, const WordFinderArgs &a, Smem &sh,
-                                            OwnerWarp &ow, OwnerState &os) {
-    using T = CellTraits<uint16_t>;
-    const int lane = threadIdx.x & 31;
-    const uint32_t pend = T::kFlag | (uint32_t)(it.dofs - 1);
-    bool want = false;
-    int left = 0, s_h = 0, q = 0;
-    if (os.tail != os.head && !os.stall) {
-        const uint32_t e = ow.fifo[os.head & (kFifo - 1)][lane];
-        s_h = (int)(e >> 16);
-        q = (int)(e & 0xffffu);
-        if (owner_apply(it, pend, s_h, q, want, left)) {
-            os.head++;
-        } else if (os.np < kPark) {
-            ow.park[os.np++][lane] = e;
-            os.head++;
-        } else {
-            os.stall = true;
-        }
-    }
-    push_task(ow, os.n_tasks, want, s_h, q, left);
-    if (os.n_tasks >= 32)
-        owner_flush(it, a, sh, ow, os, false);
-}
-
-// Hand one batch of hits (one per active lane, in CPU order by lane) to their
-// owners' FIFOs; owners out of room apply hits first.  Warp-collective.
-__device__ __forceinline__ void owner_distribute(const Item<uint16_t> &it, const WordFinderArgs &a, Smem &sh,
-                                                 OwnerWarp &ow, OwnerState &os, bool act, int s_h, int q) {
-    const int lane = threadIdx.x & 31;
-    const int owner = ((q - s_h) & it.mask) & 31;
-    const uint32_t packed = ((uint32_t)s_h << 16) | (uint32_t)q;
-    bool pending = act;
-    for (;;) {
-        const unsigned grp = __match_any_sync(0xffffffffu, pending ? owner : 32 + lane);
-        const int rank = __popc(grp & lanemask_lt());
-        const int room = __shfl_sync(0xffffffffu, kFifo - (os.tail - os.head), owner);
-        const int otail = __shfl_sync(0xffffffffu, os.tail, owner);
-        const bool place = pending && rank < room;
-        if (place)
-            ow.fifo[(otail + rank) & (kFifo - 1)][owner] = packed;
-        if (pending && rank == 0)
-            ow.cnt[owner] = (uint32_t)min(__popc(grp), room);
-        __syncwarp();
-        os.tail += (int)ow.cnt[lane];
-        ow.cnt[lane] = 0;
-        __syncwarp();
-        pending = pending && !place;
-        if (!__any_sync(0xffffffffu, pending))
-            break;
-        // owners that still have hits waiting need room
-        const unsigned needm = __reduce_or_sync(0xffffffffu, pending ? 1u << owner : 0u);
-        const bool need = (needm >> lane) & 1u;
-        if (__any_sync(0xffffffffu, need && os.stall))
-            owner_flush(it, a, sh, ow, os, false);
-        owner_round(it, a, sh, ow, os);
-    }
-    // keep FIFOs at most half full: rounds then stay busy on most lanes
-    while (__any_sync(0xffffffffu, os.tail - os.head > kFifo / 2 && !os.stall))
-        owner_round(it, a, sh, ow, os);
-}
-
-__device__ unsigned long long process_item_owner(Item<uint16_t> &it, const WordFinderArgs &a, Smem &sh,
-                                                 OwnerWarp &ow, const uint32_t *cs, const uint16_t *ents,
-                                                 int diag_alloc) {
-    const int lane = threadIdx.x & 31;
-    restart_offset(it, diag_alloc);
-    OwnerState os{0, 0, 0, false, 0};
-    Stage stg;
-    {
-        const uintptr_t sa = reinterpret_cast<uintptr_t>(it.s);
-        stg.org = reinterpret_cast<const uint4 *>(sa & ~(uintptr_t)15);
-        stg.delta = (int)(sa & 15);
-        stg.end = stg.delta + it.S;
-        stg.next = 0;
-        stg.v = stage_load(stg, 0, lane);
-    }
-    unsigned long long item_hits = 0;
-    uint32_t c_next = 0, base_next = 0;
-    if (it.S >= 3)
-        scan_words_staged(it, stg, ow, sh, cs, 0, &c_next, &base_next);
-    for (int s0 = 0; s0 <= it.S - 3; s0 += 32) {
-        const uint32_t c = c_next, base = base_next;
-        if (s0 + 32 <= it.S - 3)
-            scan_words_staged(it, stg, ow, sh, cs, s0 + 32, &c_next, &base_next);
-        uint32_t incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o)
-                incl += t;
-        }
-        const uint32_t T_ = __shfl_sync(0xffffffffu, incl, 31);
-        const uint32_t excl = incl - c;
-        const uint32_t rel = base - excl;
-        item_hits += T_;
-        auto locate = [&](uint32_t h, int *s_h, int *q) {
-            int lo = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                const uint32_t v = __shfl_sync(0xffffffffu, excl, lo + step);
-                if (v <= h)
-                    lo += step;
-            }
-            *s_h = s0 + lo;
-            const uint32_t r = __shfl_sync(0xffffffffu, rel, lo);
-            *q = h < T_ ? (int)__ldg(ents + (r + h)) : 0;
-        };
-        int s_n = 0, q_n = 0;
-        if (T_ > 0)
-            locate((uint32_t)lane, &s_n, &q_n);
-        for (uint32_t hb = 0; hb < T_; hb += 32) {
-            const bool act = hb + lane < T_;
-            const int s_h = s_n, q = q_n;
-            if (hb + 32 < T_)
-                locate(hb + 32 + lane, &s_n, &q_n);
-            owner_distribute(it, a, sh, ow, os, act, s_h, q);
-        }
-    }
-    // drain: apply every queued hit, then every extension and parked hit
-    while (__any_sync(0xffffffffu, os.tail != os.head)) {
-        if (__any_sync(0xffffffffu, os.tail != os.head && os.stall))
-            owner_flush(it, a, sh, ow, os, false);
-        owner_round(it, a, sh, ow, os);
-    }
-    owner_flush(it, a, sh, ow, os, true);
+    stage_end();
     it.dofs += it.S + it.window;
     return item_hits;
 }
@@ -980,25 +690,19 @@ __device__ unsigned long long process_item_owner(Item<uint16_t> &it, const WordF
 // Mode bit 0: offset mode (else chunk mode); bit 1: the launch's groups keep
 // their diagonal tables in global memory (same code; that instantiation asks
 // for a small shared-memory carve-out so the L1 cache holds more of the
-// tables); bit 2: owner mode (groups with shared-memory tables).  Chunk mode
-// is built for four 256-thread CTAs per SM (64 registers a thread), owner
-// mode for three (85), offset mode (large tables) for one.
+// tables).  Chunk mode is built for four 256-thread CTAs per SM (64
+// registers a thread), offset mode (large tables) for one.
 template <int Mode>
-__global__ void __launch_bounds__(256, (Mode & 4) ? 3 : ((Mode & 1) == 0 ? 4 : 1))
-    wordfinder_kernel(WordFinderArgs a) {
+__global__ void __launch_bounds__(256, (Mode & 1) == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
     constexpr bool kOffsets = (Mode & 1) != 0;
-    constexpr bool kOwner = (Mode & 4) != 0;
-    constexpr size_t kWarpBytes = kOwner ? sizeof(OwnerWarp) : sizeof(WarpQueue);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sh = *reinterpret_cast<Smem *>(smem_raw);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
-    unsigned char *warp_mem = smem_raw + sizeof(Smem) + warp * kWarpBytes;
-    WarpQueue &wq = *reinterpret_cast<WarpQueue *>(warp_mem);
-    OwnerWarp &ow = *reinterpret_cast<OwnerWarp *>(warp_mem);
+    WarpQueue &wq = reinterpret_cast<WarpQueue *>(smem_raw + sizeof(Smem))[warp];
     uint16_t *diag_s =
-        reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem) + nwarps * kWarpBytes) + warp * a.smem_diag;
+        reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * a.smem_diag;
     uint32_t *diag_g =
         a.gdiag ? a.gdiag + ((size_t)blockIdx.x * nwarps + warp) * (size_t)a.gdiag_len : nullptr;
 
@@ -1006,8 +710,6 @@ __global__ void __launch_bounds__(256, (Mode & 4) ? 3 : ((Mode & 1) == 0 ? 4 : 1
         sh.matrix[i] = c_blosum[i];
     for (int i = lane; i < a.smem_diag; i += 32)
         diag_s[i] = 0;
-    if (kOwner)
-        ow.cnt[lane] = 0;   // owner_distribute keeps it zero between batches
     const int window = a.window;
     // the 16-bit shared table starts past its limit so the first item clears it
     // offsets of the three tables a warp may use: its shared 16-bit table,
@@ -1064,11 +766,8 @@ __global__ void __launch_bounds__(256, (Mode & 4) ? 3 : ((Mode & 1) == 0 ? 4 : 1
             if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
                                   a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                if (kOwner)
-                    hits = process_item_owner(it, a, sh, ow, cs, ents, a.smem_diag);
-                else
-                    hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
-                                    : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
+                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
+                                : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
                 dofs_s = it.dofs;
             } else if (window + S <= CellTraits<uint16_t>::kLimit) {
                 Item<uint16_t> it{sp, S, j, reinterpret_cast<uint16_t *>(diag_g), G.diag_len - 1, dofs_h,
@@ -1100,24 +799,9 @@ __global__ void __launch_bounds__(256, (Mode & 4) ? 3 : ((Mode & 1) == 0 ? 4 : 1
     }
 }
 
-size_t wordfinder_smem_bytes(int mode, int threads, int smem_diag) {
-    const size_t per_warp = (mode & 4) ? sizeof(OwnerWarp) : sizeof(WarpQueue);
-    return sizeof(Smem) + (size_t)(threads / 32) * (per_warp + (size_t)smem_diag * sizeof(uint16_t));
+size_t wordfinder_smem_bytes(int threads, int smem_diag) {
+    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + (size_t)smem_diag * sizeof(uint16_t));
 }
-
-namespace {
-template <int M>
-const void *kernel_of() { return (const void *)wordfinder_kernel<M>; }
-const void *kernel_for(int mode) {
-    switch (mode & 7) {
-    case 0: return kernel_of<0>();
-    case 1: return kernel_of<1>();
-    case 2: return kernel_of<2>();
-    case 3: return kernel_of<3>();
-    default: return kernel_of<4>();    // owner mode: shared tables, chunk location
-    }
-}
-}  // namespace
 
 cudaError_t wordfinder_configure() {
     // opt in to the largest shared-memory carve-out; launches size their own.
@@ -1128,11 +812,12 @@ cudaError_t wordfinder_configure() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int modes[5] = {0, 1, 2, 3, 4};
-    for (int m : modes) {
-        cudaError_t e = cudaFuncSetAttribute(kernel_for(m), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    const void *k[4] = {(const void *)wordfinder_kernel<0>, (const void *)wordfinder_kernel<1>,
+                        (const void *)wordfinder_kernel<2>, (const void *)wordfinder_kernel<3>};
+    for (int m = 0; m < 4; ++m) {
+        cudaError_t e = cudaFuncSetAttribute(k[m], cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         if (e == cudaSuccess && (m & 2))
-            e = cudaFuncSetAttribute(kernel_for(m), cudaFuncAttributePreferredSharedMemoryCarveout, 40);
+            e = cudaFuncSetAttribute(k[m], cudaFuncAttributePreferredSharedMemoryCarveout, 40);
         if (e != cudaSuccess)
             return e;
     }
@@ -1140,19 +825,23 @@ cudaError_t wordfinder_configure() {
 }
 
 cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel_for(mode), threads,
-                                                         wordfinder_smem_bytes(mode, threads, smem_diag));
+    const size_t smem = wordfinder_smem_bytes(threads, smem_diag);
+    switch (mode & 3) {
+    case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
+    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem);
+    case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<2>, threads, smem);
+    default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<3>, threads, smem);
+    }
 }
 
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream) {
-    const size_t smem = wordfinder_smem_bytes(mode, threads, a.smem_diag);
-    switch (mode & 7) {
+    const size_t smem = wordfinder_smem_bytes(threads, a.smem_diag);
+    switch (mode & 3) {
     case 0: wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a); break;
     case 1: wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a); break;
     case 2: wordfinder_kernel<2><<<blocks, threads, smem, stream>>>(a); break;
-    case 3: wordfinder_kernel<3><<<blocks, threads, smem, stream>>>(a); break;
-    default: wordfinder_kernel<4><<<blocks, threads, smem, stream>>>(a); break;
+    default: wordfinder_kernel<3><<<blocks, threads, smem, stream>>>(a); break;
     }
     return cudaGetLastError();
 }

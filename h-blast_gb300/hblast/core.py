@@ -333,7 +333,7 @@ class Batch:
         return self
 
     def set_mode(self, mode: int, group: int = -1) -> "Batch":
-        """0 = chunk mode, 1 = offset mode, 2 = owner mode, for one group or all (before the first search)."""
+        """0 = chunk mode, 1 = offset mode, for one group or all (before the first search)."""
         _check(lib().hbg_batch_set_mode(self.handle, group, mode))
         return self
 

@@ -318,7 +318,7 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
             for (int y = 0; y < 20; ++y)
                 for (int z = 0; z < 20; ++z)
                     std_entries += count[(kStd[x] << 10) | (kStd[y] << 5) | kStd[z]];
-        G.mode = (double)std_entries / 8000.0 >= mode_hits ? 1 : kDefaultMode;
+        G.mode = (double)std_entries / 8000.0 >= mode_hits ? 1 : 0;
     });
     int64_t entry_pos = 0;
     for (int32_t g = 0; g < n_groups; ++g) {

@@ -239,14 +239,10 @@ int hbg_batch_lookup_table(const hbg_batch *batch, int32_t g, uint32_t *cells,
                            int32_t *first_query, int32_t *n_queries, int32_t *query_start);
 
 /* Choose how group g (all groups when g < 0) applies its hits: mode 0 =
- * chunk mode (32 offsets compacted at a time, hits of one diagonal ordered
- * inside each batch of 32), 1 = offset mode (one subject offset at a time,
- * lanes over its cell; for very dense groups), 2 = owner mode (the default:
- * each lane owns the diagonals congruent to it mod 32 and applies their hits
- * from a per-lane queue; needs a shared-memory diagonal table, i.e. a group of
- * at most 2008 letters with the default window -- longer groups run chunk
- * mode).  Results do not depend on the choice.  Call before the batch's first
- * search. */
+ * chunk mode (32 offsets compacted at a time; best for sparse groups), 1 =
+ * offset mode (one subject offset at a time, lanes over its cell; best for
+ * dense groups).  The builder picks by expected hits per offset; results do
+ * not depend on the choice.  Call before the batch's first search. */
 int hbg_batch_set_mode(hbg_batch *batch, int32_t g, int32_t mode);
 
 /* Work-unit and table placement knobs for tuning (results do not depend on

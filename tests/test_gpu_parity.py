@@ -88,7 +88,7 @@ def test_long_query_tables(built, qlen):
     check(res, pqs, db.residues, db.offsets)
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode", [0, 1])
 def test_both_hit_modes(small_db, mode):
     qs, db, gdb = small_db
     pqs = [hblast.ProteinQuery.blastp(q) for q in qs]

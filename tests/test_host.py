@@ -183,10 +183,9 @@ def test_tuning_calls_validate_before_upload(built):
         with pytest.raises(hblast.HblastError):
             b.tune(*bad)
     b.tune(64, True).tune(0, False)        # valid values; global tables stay chosen
-    for bad in (3, -1):
-        with pytest.raises(hblast.HblastError):
-            b.set_mode(bad)
-    b.set_mode(1).set_mode(0, 0).set_mode(2, 0)
+    with pytest.raises(hblast.HblastError):
+        b.set_mode(2)
+    b.set_mode(1).set_mode(0, 0)
     b.close()
 
 
