@@ -48,9 +48,11 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="hblast", choices=["hblast", "reference"])
-    p.add_argument("--config", default="batched", choices=["batched", "plain", "blastx", "served", "autotune", "ingest"])
-    p.add_argument("--rates", default="2,5,10,20", help="served: Poisson arrival rates (queries/s)")
-    p.add_argument("--requests", type=int, default=60, help="served: requests per rate")
+    p.add_argument("--config", default="batched",
+                   choices=["batched", "plain", "blastx", "scan", "served", "autotune", "ingest"])
+    p.add_argument("--rates", default="50,200,1000,2000", help="served: Poisson arrival rates (queries/s)")
+    p.add_argument("--requests", type=int, default=1000, help="served: requests per rate")
+    p.add_argument("--forms", default="served,plain", help="served: forms to run (served, served_2, served_fifo, plain)")
     p.add_argument("--subjects", type=int, default=0, help="override the database size (testing)")
     p.add_argument("--queries", type=int, default=0, help="override the number of queries (testing)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
@@ -77,6 +79,14 @@ def workload(cfg: str, rank: int, n_subjects: int, n_queries: int):
         desc = dict(workload="batched blastx: 128 nucleotide queries of 300..3000 nt (GC 0.5, planted ORFs matching "
                              "database proteins at 40..70% identity), six frames, vs the 2,000,000-subject database")
         return nts, db, desc
+    if cfg == "scan":
+        n = n_queries or 1
+        qs = synth.heavy_tailed_queries(rank, n)
+        db = synth.large_db(rank, n_subjects or 10_000_000, donors=qs)
+        desc = dict(workload=f"scan-bound blastp: {n} heavy-tailed quer{'y' if n == 1 else 'ies'} (lognormal median "
+                             f"350, sigma 1.0; {sum(len(q) for q in qs)} letters) vs {db.n:,} lognormal subjects "
+                             "(median 300, sigma 0.6, 30..5000), 1% planted 50..300 aa at 30..60% identity")
+        return qs, db, desc
     if cfg == "plain":
         qs, db = synth.plain_blastp(seed=rank, n_subjects=n_subjects or 20000)
         desc = dict(workload="plain blastp: 1 query of 300 aa vs 20,000 lognormal subjects (median 300, "
@@ -221,9 +231,7 @@ def served_arm(args):
     import hblast
     from hblast import synth
     n_sub = args.subjects or 10_000_000
-    rng = np.random.default_rng(0)
-    db = synth.make_db(rng, n_sub, 300, 0.6, 30, 5000, 0.01, [synth.random_letters(rng, 400)],
-                       lambda r: r.integers(50, 301), lambda r: r.uniform(0.3, 0.6))
+    db = synth.large_db(0, n_sub)
     gdb = hblast.Database(db.residues, db.offsets)
     ssum = int(db.offsets[-1])
     xd6, cu6 = np.full(6, 16, np.int32), np.full(6, 41, np.int32)
@@ -239,6 +247,7 @@ def served_arm(args):
                     "served_2": "as served, 2 batches in flight",
                     "served_fifo": "arrival-order admission, no letter cap, 2 batches in flight",
                     "plain": "one query per launch, one at a time, arrival order"}
+    forms = {k: v for k, v in forms.items() if k in args.forms.split(",")}
     for form, so in forms.items():
         res_form = []
         for rate in rates:
@@ -286,7 +295,8 @@ def served_arm(args):
             res_form.append({"rate": rate, "p50_ms": float(np.percentile(lat, 50)),
                              "p99_ms": float(np.percentile(lat, 99)), "wall_s": wall,
                              "queries_per_s": len(lat) / wall, "residues_per_s": letters * ssum / wall,
-                             "batches": c["batches"], "largest_batch": c["largest_batch"]})
+                             "batches": c["batches"], "largest_batch": c["largest_batch"],
+                             "requeued": c["requeued"]})
             print(json.dumps({"form": form, **res_form[-1]}), file=sys.stderr, flush=True)
         out[form] = res_form
     print(json.dumps(out), flush=True)

@@ -36,7 +36,8 @@ int fail(int code, const std::string &msg) {
     do {                                                                          \
         cudaError_t e_ = (call);                                                  \
         if (e_ != cudaSuccess)                                                    \
-            return fail(HBG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            return fail(e_ == cudaErrorMemoryAllocation ? HBG_ERR_NOMEM : HBG_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));      \
     } while (0)
 
 int bits_for(int64_t v) {
@@ -67,9 +68,16 @@ DevicePool &pool() {
     return *p;
 }
 
+// Allocation failures injected for tests (hbg_debug_fail_allocations): the
+// next this many dalloc calls report cudaErrorMemoryAllocation.
+std::atomic<int32_t> g_fail_allocs{0};
+
 template <class T>
 cudaError_t dalloc(T **p, size_t n) {
     *p = nullptr;
+    for (int32_t k = g_fail_allocs.load(); k > 0;)
+        if (g_fail_allocs.compare_exchange_weak(k, k - 1))
+            return cudaErrorMemoryAllocation;
     if (n == 0)
         n = 1;
     const size_t bytes = n * sizeof(T);
@@ -89,8 +97,10 @@ cudaError_t dalloc(T **p, size_t n) {
     }
     void *q = nullptr;
     cudaError_t e = cudaMalloc(&q, bytes);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // a failed allocation must not surface at a later launch check
         return e;
+    }
     std::lock_guard<std::mutex> lock(P.mu);
     P.size_of[q] = bytes;
     *p = (T *)q;
@@ -253,12 +263,39 @@ int64_t batch_device_bytes(const hbg::HostBatch &h) {
                      h.cells.size() * 4 + h.entries.size() * 2 + h.pv.size() * 4 + h.query_cells.size() * 2);
 }
 
+void free_batch_device(hbg_batch *b) {
+    dfree_idle(b->d_groups);
+    dfree_idle(b->d_ctx);
+    dfree_idle(b->d_queries);
+    dfree_idle(b->d_letters);
+    dfree_idle(b->d_ctx_of);
+    dfree_idle(b->d_cells);
+    dfree_idle(b->d_entries);
+    dfree_idle(b->d_pv);
+    dfree_idle(b->d_qcells);
+    dfree_idle(b->d_group_list);
+}
+
+int upload_batch_buffers(hbg_batch *b, int device);
+
+// Upload at the first search; a failed upload gives back what it allocated,
+// so the batch can be searched again later.
 int upload_batch(hbg_batch *b, int device) {
     if (b->device == device)
         return HBG_OK;
     if (b->device >= 0)
         return fail(HBG_ERR_STATE, "batch already resident on another device");
     DeviceScope ds(device);
+    const int rc = upload_batch_buffers(b, device);
+    if (rc != HBG_OK) {
+        cudaDeviceSynchronize();   // copies already issued may still read the host vectors
+        free_batch_device(b);
+        b->device = -1;
+    }
+    return rc;
+}
+
+int upload_batch_buffers(hbg_batch *b, int device) {
     const hbg::HostBatch &h = b->host;
     CU(dalloc(&b->d_groups, h.groups.size()));
     CU(dalloc(&b->d_ctx, h.contexts.size()));
@@ -367,6 +404,12 @@ int plan_launches(const hbg_batch *b, const hbg_gpu_options &o, int device, std:
     return HBG_OK;
 }
 
+void drop_graph(hbg_result *r) {
+    if (r->graph_exec)
+        cudaGraphExecDestroy(r->graph_exec);
+    r->graph_exec = nullptr;
+}
+
 void free_result_device(hbg_result *r) {
     if (r->graph_exec)
         cudaGraphExecDestroy(r->graph_exec);
@@ -401,25 +444,33 @@ int prepare_result(hbg_result *r, int64_t cap) {
         for (auto &e : r->ev)
             CU(cudaEventCreate(&e));
     }
+    // a failed allocation below leaves the recorded size at 0, so the next
+    // search allocates again instead of using a missing buffer
     if (r->n_counters < 1 + 6 * nq + ng) {   // first use, or a larger batch
+        drop_graph(r);
         dfree(r->d_counters);
         if (r->h_counters)
             cudaFreeHost(r->h_counters);
         r->h_counters = nullptr;
+        r->n_counters = 0;
+        CU(dalloc(&r->d_counters, 1 + 6 * nq + ng));
+        CU(cudaMallocHost((void **)&r->h_counters, (1 + 6 * nq + ng) * sizeof(unsigned long long)));
         r->n_counters = 1 + 6 * nq + ng;
-        CU(dalloc(&r->d_counters, r->n_counters));
-        CU(cudaMallocHost((void **)&r->h_counters, r->n_counters * sizeof(unsigned long long)));
     }
     r->gdiag_len = global_diag_len(h, r->db);
     if (r->gdiag_len > 0) {
         const int64_t need = (int64_t)r->blocks * (r->threads / 32) * r->gdiag_len;
         if (need > r->gdiag_entries) {
+            drop_graph(r);
             dfree(r->d_gdiag);
+            r->gdiag_entries = 0;
             CU(dalloc(&r->d_gdiag, (size_t)need));
             r->gdiag_entries = need;
         }
     }
     if (cap > r->cap) {
+        drop_graph(r);
+        r->cap = 0;
         dfree(r->d_raw);
         dfree(r->d_sorted);
         dfree(r->d_keys);
@@ -533,12 +584,6 @@ int enqueue_search(hbg_result *r) {
     CU(cudaMemcpyAsync(r->h_counters, r->d_counters, r->n_counters * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, st));
     return HBG_OK;
-}
-
-void drop_graph(hbg_result *r) {
-    if (r->graph_exec)
-        cudaGraphExecDestroy(r->graph_exec);
-    r->graph_exec = nullptr;
 }
 
 // Launch a search.  A result that is launched again on the same non-default
@@ -1169,16 +1214,7 @@ int hbg_batch_destroy(hbg_batch *b) {
         // searches of this batch may run on any stream: wait for the device
         // (as cudaFree would), then keep the buffers for reuse
         cudaDeviceSynchronize();
-        dfree_idle(b->d_groups);
-        dfree_idle(b->d_ctx);
-        dfree_idle(b->d_queries);
-        dfree_idle(b->d_letters);
-        dfree_idle(b->d_ctx_of);
-        dfree_idle(b->d_cells);
-        dfree_idle(b->d_entries);
-        dfree_idle(b->d_pv);
-        dfree_idle(b->d_qcells);
-        dfree_idle(b->d_group_list);
+        free_batch_device(b);
     }
     delete b;
     return HBG_OK;
@@ -1309,13 +1345,17 @@ int hbg_result_sync(hbg_result *r) {
     CU(cudaStreamSynchronize(r->stream));
     unsigned long long n = r->h_counters[0];
     if ((int64_t)n > r->cap) {
-        // the HSP buffer was too small: relaunch once with the exact size
+        // the HSP buffer was too small: relaunch once with the exact size.  If
+        // that cannot be set up, nothing of this search runs any more and the
+        // result may be relaunched (or reused for another batch) later.
         int rc = prepare_result(r, (int64_t)n);
-        if (rc != HBG_OK)
+        if (rc == HBG_OK)
+            rc = launch_search(r);
+        if (rc != HBG_OK) {
+            cudaStreamSynchronize(r->stream);
+            r->launched = false;
             return rc;
-        rc = launch_search(r);
-        if (rc != HBG_OK)
-            return rc;
+        }
         CU(cudaStreamSynchronize(r->stream));
         n = r->h_counters[0];
         if ((int64_t)n > r->cap)
@@ -1589,5 +1629,12 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
     // per-query extension and kept counts follow the HSP count in d_counts
     CU(cudaMemcpyAsync(d_counts + 1, q_ext, sizeof(unsigned long long) * (size_t)(2 * nq),
                        cudaMemcpyDeviceToDevice, st));
+    return HBG_OK;
+}
+
+extern "C" int hbg_debug_fail_allocations(int32_t count) {
+    if (count < 0)
+        return fail(HBG_ERR_INVALID, "hbg_debug_fail_allocations: negative count");
+    g_fail_allocs.store(count);
     return HBG_OK;
 }

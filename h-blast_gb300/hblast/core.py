@@ -116,7 +116,9 @@ _SIGS = {
     "hbg_server_wait": ([_P, C.c_int64, C.c_int32, C.POINTER(C.c_int64)], C.c_int),
     "hbg_server_take": ([_P, C.c_int64, _P, C.c_int64, C.POINTER(QueryStats), C.POINTER(C.c_double)], C.c_int),
     "hbg_server_counters": ([_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
+    "hbg_server_requeued": ([_P, C.POINTER(C.c_int64)], C.c_int),
     "hbg_server_destroy": ([_P], C.c_int),
+    "hbg_debug_fail_allocations": ([C.c_int32], C.c_int),
 }
 
 _lib = None
@@ -154,6 +156,12 @@ def device_count() -> int:
     n = C.c_int32(0)
     rc = lib().hbg_device_count(C.byref(n))
     return n.value if rc == HBG_OK else 0
+
+
+def fail_allocations(count: int) -> None:
+    """Test hook (hbg_debug_fail_allocations): the library's next `count` device
+    allocations fail as if the device were out of memory."""
+    _check(lib().hbg_debug_fail_allocations(count))
 
 
 def default_options(**kw) -> GpuOptions:
@@ -477,9 +485,10 @@ class Server:
                          good_init_extends=st.good_init_extends, subjects_passed=st.subjects_passed), lat.value
 
     def counters(self):
-        b, q, l = C.c_int64(), C.c_int64(), C.c_int64()
+        b, q, l, rq = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
         _check(lib().hbg_server_counters(self.handle, C.byref(b), C.byref(q), C.byref(l)))
-        return dict(batches=b.value, queries=q.value, largest_batch=l.value)
+        _check(lib().hbg_server_requeued(self.handle, C.byref(rq)))
+        return dict(batches=b.value, queries=q.value, largest_batch=l.value, requeued=rq.value)
 
     def close(self):
         if self.handle:

@@ -235,3 +235,15 @@ def heavy_tailed_queries(seed: int, n: int):
     rng = np.random.default_rng(seed + 7)
     lens = lognormal_lengths(rng, n, 350, 1.0, 30, 35000)
     return [random_letters(rng, int(L)) for L in lens]
+
+
+def large_db(seed: int = 0, n_subjects: int = 10_000_000, donors=None):
+    """The 10,000,000-subject database of the heavy-tailed and served workloads (lognormal
+    lengths, median 300, sigma 0.6, 30..5000; 1% carry a 50..300 aa segment of a donor at
+    30..60% identity; donors default to one random 400-aa protein)."""
+    rng = np.random.default_rng(seed)
+    if not donors:
+        donors = [random_letters(rng, 400)]
+    return make_db(rng, n_subjects, 300, 0.6, 30, 5000, 0.01, list(donors),
+                   lambda r: r.integers(50, 301), lambda r: r.uniform(0.3, 0.6))
+

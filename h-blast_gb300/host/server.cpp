@@ -16,6 +16,15 @@
 // searched independently (own diagonals, own bounds), so every request's
 // result equals a search of it alone.
 //
+// Memory: requests are chosen by an estimate of their device bytes; once the
+// batch is built its exact need (hbg_mem_required: lookup tables, HSP and
+// sort buffers, diagonal scratch) is checked against the budget left by the
+// batches in flight and against the device's free memory.  A batch that does
+// not fit -- or whose search fails with HBG_ERR_NOMEM -- goes back to the
+// front of the queue and is retried with half as many requests; a lone
+// request that does not fit beside running batches waits for them to end.
+// Only a request that fails alone on an otherwise idle device fails.
+//
 // This takes the place of H-BLAST's CPU/GPU load balancer and its
 // one-process-per-GPU query split (NF/functions.cpp:51-140,1221-1827;
 // scripts/H-BLASTM:212-305).
@@ -76,7 +85,9 @@ struct hbg_server {
     std::vector<Slot> slots;
     int64_t next_id = 1;
     int64_t inflight_bytes = 0;
-    int64_t batches = 0, completed = 0, largest = 0;
+    int64_t batches = 0, completed = 0, largest = 0, requeued = 0;
+    int32_t admit_cap = 0;   // > 0: the next batch takes at most this many requests
+    bool hold = false;       // a lone request waits for a running batch to end
     bool stop = false;
     std::thread th;
 };
@@ -97,6 +108,44 @@ int64_t estimate_bytes(int64_t qlen, int64_t db_res) {
     // query's cell counts (64 KiB), its share of group cells (132 KiB per
     // 2000 letters), and HSP buffers (raw + ordered + sort keys, ~100 B each)
     return 65536 + qlen * (40 + 5 + 70) + estimate_hsps(qlen, db_res) * 100;
+}
+
+// Device memory left free beside a new batch (the runtime, other streams).
+constexpr int64_t kFreeReserve = (int64_t)256 << 20;
+
+bool others_busy(const hbg_server *S, const Slot &me) {
+    for (const Slot &sl : S->slots)
+        if (&sl != &me && sl.busy)
+            return true;
+    return false;
+}
+
+// Requests of a batch that did not fit go back to the front of the queue, in
+// their order.  Returns false when they cannot fit at all (alone, with
+// nothing else running): the caller fails them.
+bool back_off(hbg_server *S, const std::vector<int64_t> &ids, bool others) {
+    if (ids.size() > 1)
+        S->admit_cap = std::max<int32_t>(1, (int32_t)ids.size() / 2);
+    else if (others)
+        S->hold = true;
+    else
+        return false;
+    for (auto it = ids.rbegin(); it != ids.rend(); ++it)
+        S->pending.push_front(*it);
+    S->requeued += (int64_t)ids.size();
+    S->cv_work.notify_one();
+    return true;
+}
+
+void fail_requests(hbg_server *S, const std::vector<int64_t> &ids, int rc) {
+    for (int64_t id : ids) {
+        Request &r = S->reqs[id];
+        r.status = rc;
+        r.done = true;
+        r.latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - r.t0).count();
+        S->completed++;
+    }
+    S->cv_done.notify_all();
 }
 
 bool valid_query(const hbg_query *q) {
@@ -136,6 +185,15 @@ void finish_slot(hbg_server *S, Slot &sl, std::unique_lock<std::mutex> &lk) {
     sl.batch = nullptr;
     const auto now = Clock::now();
     lk.lock();
+    S->inflight_bytes -= sl.bytes;
+    sl.bytes = 0;
+    sl.busy = false;
+    S->hold = false;                   // a waiting lone request may fit now
+    if (rc == HBG_ERR_NOMEM && back_off(S, sl.ids, others_busy(S, sl))) {
+        sl.ids.clear();
+        S->cv_done.notify_all();
+        return;
+    }
     for (size_t k = 0; k < sl.ids.size(); ++k) {
         Request &r = S->reqs[sl.ids[k]];
         r.status = rc;
@@ -147,14 +205,11 @@ void finish_slot(hbg_server *S, Slot &sl, std::unique_lock<std::mutex> &lk) {
         r.done = true;
         S->completed++;
     }
-    S->inflight_bytes -= sl.bytes;
     sl.ids.clear();
-    sl.bytes = 0;
-    sl.busy = false;
     S->cv_done.notify_all();
 }
 
-void launch_slot(hbg_server *S, Slot &sl, std::vector<int64_t> ids, int64_t bytes,
+void launch_slot(hbg_server *S, Slot &sl, std::vector<int64_t> ids, int64_t est,
                  std::unique_lock<std::mutex> &lk) {
     std::vector<hbg_query> qs(ids.size());
     int64_t qres = 0;
@@ -165,34 +220,63 @@ void launch_slot(hbg_server *S, Slot &sl, std::vector<int64_t> ids, int64_t byte
         qres += (int64_t)r.seq.size();
     }
     sl.ids = ids;
-    sl.bytes = bytes;
+    sl.bytes = est;
     sl.busy = true;
-    S->inflight_bytes += bytes;
+    S->inflight_bytes += est;
+    lk.unlock();
+    const int64_t cap = estimate_hsps(qres, S->db_residues);
+    int rc = hbg_batch_create(qs.data(), (int32_t)qs.size(), &S->wp, S->so.max_group_len, &sl.batch);
+    int64_t need = 0;
+    size_t free_b = 0, total_b = 0;
+    if (rc == HBG_OK)
+        rc = hbg_mem_required(S->db, sl.batch, cap, &need);
+    if (rc == HBG_OK && cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = (size_t)INT64_MAX;        // unknown: rely on the budget and on allocation failures
+    }
+    lk.lock();
+    const bool others = others_busy(S, sl);
+    if (rc == HBG_OK) {
+        const bool over = need > S->so.memory_budget - (S->inflight_bytes - est) ||
+                          need + kFreeReserve > (int64_t)std::min<size_t>(free_b, (size_t)INT64_MAX);
+        if (over && (ids.size() > 1 || others)) {
+            S->inflight_bytes -= est;
+            sl.busy = false;
+            sl.ids.clear();
+            sl.bytes = 0;
+            hbg_batch *b = sl.batch;
+            sl.batch = nullptr;
+            back_off(S, ids, others);
+            lk.unlock();
+            hbg_batch_destroy(b);
+            lk.lock();
+            return;
+        }
+        S->inflight_bytes += need - est;    // account the exact size from now on
+        sl.bytes = need;
+        lk.unlock();
+        rc = hbg_search(S->db, sl.batch, &S->opt, cap, sl.stream, &sl.res);
+        lk.lock();
+    }
+    if (rc != HBG_OK) {
+        S->inflight_bytes -= sl.bytes;
+        sl.busy = false;
+        sl.ids.clear();
+        sl.bytes = 0;
+        hbg_batch *b = sl.batch;
+        sl.batch = nullptr;
+        if (!(rc == HBG_ERR_NOMEM && back_off(S, ids, others_busy(S, sl))))
+            fail_requests(S, ids, rc);
+        if (b) {
+            lk.unlock();
+            hbg_batch_destroy(b);
+            lk.lock();
+        }
+        return;
+    }
     S->batches++;
     S->largest = std::max<int64_t>(S->largest, (int64_t)ids.size());
-    lk.unlock();
-    int rc = hbg_batch_create(qs.data(), (int32_t)qs.size(), &S->wp, S->so.max_group_len, &sl.batch);
-    if (rc == HBG_OK)
-        rc = hbg_search(S->db, sl.batch, &S->opt, estimate_hsps(qres, S->db_residues), sl.stream, &sl.res);
-    lk.lock();
-    if (rc != HBG_OK) {
-        // fail these requests; the slot is free again
-        if (sl.batch) {
-            hbg_batch_destroy(sl.batch);
-            sl.batch = nullptr;
-        }
-        for (int64_t id : ids) {
-            Request &r = S->reqs[id];
-            r.status = rc;
-            r.done = true;
-            r.latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - r.t0).count();
-            S->completed++;
-        }
-        S->inflight_bytes -= bytes;
-        sl.ids.clear();
-        sl.busy = false;
-        S->cv_done.notify_all();
-    }
+    S->admit_cap = 0;
 }
 
 void dispatcher(hbg_server *S) {
@@ -218,7 +302,7 @@ void dispatcher(hbg_server *S) {
                 free_slot = &sl;
                 break;
             }
-        if (free_slot && !S->pending.empty()) {
+        if (free_slot && !S->pending.empty() && !S->hold) {
             std::vector<int64_t> cand(S->pending.begin(), S->pending.end());
             if (S->so.shortest_first_ms > 0) {
                 const Clock::time_point now = Clock::now();
@@ -233,8 +317,10 @@ void dispatcher(hbg_server *S) {
             }
             std::vector<int64_t> ids;
             int64_t bytes = 0, letters = 0;
+            const int32_t max_q = S->admit_cap > 0 ? std::min(S->admit_cap, S->so.max_batch_queries)
+                                                   : S->so.max_batch_queries;
             for (int64_t id : cand) {
-                if ((int32_t)ids.size() >= S->so.max_batch_queries)
+                if ((int32_t)ids.size() >= max_q)
                     break;
                 const Request &r = S->reqs[id];
                 const int64_t room = S->so.memory_budget - S->inflight_bytes - bytes;
@@ -413,6 +499,15 @@ int hbg_server_counters(const hbg_server *S, int64_t *batches, int64_t *queries,
         *queries = S->completed;
     if (largest)
         *largest = S->largest;
+    return HBG_OK;
+}
+
+int hbg_server_requeued(const hbg_server *S, int64_t *requeued) {
+    if (!S || !requeued)
+        return HBG_ERR_INVALID;
+    hbg_server *m = const_cast<hbg_server *>(S);
+    std::lock_guard<std::mutex> lock(m->mu);
+    *requeued = S->requeued;
     return HBG_OK;
 }
 

@@ -366,6 +366,13 @@ int hbg_server_take(hbg_server *s, int64_t ticket, hbg_hsp *out, int64_t cap,
 int hbg_server_counters(const hbg_server *s, int64_t *batches, int64_t *queries,
                         int64_t *largest_batch);
 
+/* Requests put back in the queue since creation because their batch did not
+ * fit (the budget, the device's free memory, or an allocation that failed);
+ * each was searched again later.  No counterpart in the reference: H-BLAST
+ * checks memory before it launches (H_BLAST_check_memory, h_blast.cu:1280-1349)
+ * and sends a search that does not fit to the CPU (NF/functions.cpp:1518-1530). */
+int hbg_server_requeued(const hbg_server *s, int64_t *requeued);
+
 /* Finish every admitted request, then stop. */
 int hbg_server_destroy(hbg_server *s);
 
@@ -407,6 +414,14 @@ int hbg_server_destroy(hbg_server *s);
 int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const hbg_gpu_options *opt,
                       hbg_hsp *d_hsps, int64_t hsp_cap, unsigned long long *d_counts,
                       void *stream);
+
+/* ---- testing --------------------------------------------------------------- */
+
+/* Make the library's next `count` device allocations fail as if the device
+ * were out of memory (HBG_ERR_NOMEM from the call that needed them); 0 stops
+ * it.  For tests of the out-of-memory paths without exhausting a shared GPU.
+ * No counterpart in the reference. */
+int hbg_debug_fail_allocations(int32_t count);
 
 /* ---- one-call helper ------------------------------------------------------ */
 

@@ -76,3 +76,54 @@ def test_memory_budget_limits_batches(served):
         assert np.array_equal(hsps, alone(gdb, hblast.ProteinQuery.blastp(q))[0])
     assert srv.counters()["largest_batch"] == 1
     srv.close()
+
+
+def test_allocation_failures_requeue_requests(served):
+    """Device allocations that fail (injected: the library's next allocations
+    report out-of-memory) put a batch's requests back in the queue; they are
+    searched again and complete with the same HSPs as alone.  The reference's
+    counterpart is the CPU fallback when GPU memory falls short
+    (NF/functions.cpp:1518-1530)."""
+    qs, nts, db, gdb = served
+    refs = [alone(gdb, hblast.ProteinQuery.blastp(q)) for q in qs[:8]]
+    srv = hblast.Server(gdb, max_inflight=1, max_batch_queries=8)
+    hblast.fail_allocations(3)
+    try:
+        ts = [srv.submit(hblast.ProteinQuery.blastp(q)) for q in qs[:8]]
+        got = [srv.take(t) for t in ts]
+    finally:
+        hblast.fail_allocations(0)
+    for (hsps, stats, _), (ref, ref_stats) in zip(got, refs):
+        assert np.array_equal(hsps, ref)
+        assert stats == ref_stats
+    c = srv.counters()
+    assert c["requeued"] >= 1 and c["queries"] == 8
+    srv.close()
+
+
+def test_search_out_of_memory_is_recoverable(served):
+    """A search whose buffers cannot be allocated returns HBG_ERR_NOMEM and
+    leaves nothing broken: the same batch and result search correctly
+    afterwards, including a relaunch whose larger HSP buffer fails first."""
+    qs, nts, db, gdb = served
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs[:4]]
+    ref = hblast.search(gdb, hblast.Batch.proteins(pqs))
+    batch = hblast.Batch.proteins(pqs)
+    hblast.fail_allocations(1)
+    with pytest.raises(hblast.HblastError) as e:
+        hblast.search(gdb, batch)
+    assert e.value.code == hblast.core.HBG_ERR_NOMEM
+    hblast.fail_allocations(0)
+    assert np.array_equal(hblast.search(gdb, batch).hsps, ref.hsps)
+    # relaunch on HSP-buffer overflow: its allocation fails, then succeeds
+    s = hblast.Searcher(gdb, batch, hsp_capacity=1)
+    s.launch(None)
+    hblast.fail_allocations(1)
+    with pytest.raises(hblast.HblastError) as e:
+        s.wait()
+    assert e.value.code == hblast.core.HBG_ERR_NOMEM
+    hblast.fail_allocations(0)
+    s.launch(None)
+    s.wait()
+    assert np.array_equal(s.result().hsps, ref.hsps)
+    s.close()

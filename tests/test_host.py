@@ -197,3 +197,12 @@ def test_autotune_table_round_trip(tmp_path):
     assert back[0].best == rows[0].best
     assert autotune.choice_for(100, back) == rows[0].best
     assert autotune.choice_for(5000, back) == autotune.Choice(0, 0, 256)
+
+
+def test_allocation_failure_hook_validates(built):
+    """The out-of-memory test hook takes a count and is switched off with 0
+    (no device needed)."""
+    with pytest.raises(hblast.HblastError):
+        hblast.fail_allocations(-1)
+    hblast.fail_allocations(2)
+    hblast.fail_allocations(0)
