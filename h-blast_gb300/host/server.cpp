@@ -58,6 +58,7 @@ struct Request {
     std::vector<hbg_hsp> hsps;
     hbg_query_stats stats{0, 0, 0, 0};
     double latency_ms = 0;
+    int32_t lone_failures = 0;   // out-of-memory failures while alone on an otherwise idle device
 };
 
 struct Slot {
@@ -120,15 +121,20 @@ bool others_busy(const hbg_server *S, const Slot &me) {
     return false;
 }
 
+// A request that runs out of device memory alone on an otherwise idle device
+// is tried this many more times (the shortfall may be another process's and
+// pass) before it fails.
+constexpr int32_t kLoneRetries = 3;
+
 // Requests of a batch that did not fit go back to the front of the queue, in
 // their order.  Returns false when they cannot fit at all (alone, with
-// nothing else running): the caller fails them.
+// nothing else running, after kLoneRetries retries): the caller fails them.
 bool back_off(hbg_server *S, const std::vector<int64_t> &ids, bool others) {
     if (ids.size() > 1)
         S->admit_cap = std::max<int32_t>(1, (int32_t)ids.size() / 2);
     else if (others)
         S->hold = true;
-    else
+    else if (++S->reqs[ids[0]].lone_failures > kLoneRetries)
         return false;
     for (auto it = ids.rbegin(); it != ids.rend(); ++it)
         S->pending.push_front(*it);
