@@ -1056,11 +1056,44 @@ int hbg_batch_create(const hbg_query *queries, int32_t n_queries, const hbg_word
     return finish_batch(qs, params, max_group_len, out);
 }
 
+int hbg_seg_default_params(hbg_seg_params *p) {
+    if (!p)
+        return fail(HBG_ERR_INVALID, "hbg_seg_default_params: null argument");
+    p->window = 12;
+    p->pad = 0;
+    p->locut = 2.2;
+    p->hicut = 2.5;
+    return HBG_OK;
+}
+
+static bool valid_seg(const hbg_seg_params *p) {
+    return p && p->window >= 1 && p->window <= 1000 && p->locut >= 0 && p->hicut >= p->locut;
+}
+
+int hbg_seg_mask(uint8_t *seq, int32_t len, const hbg_seg_params *p, int64_t *n_masked) {
+    if (!seq || len < 0 || !valid_seg(p))
+        return fail(HBG_ERR_INVALID, "hbg_seg_mask: null sequence, negative length or bad parameters");
+    const int64_t n = hbg::seg_mask(seq, len, p->window, p->locut, p->hicut);
+    if (n_masked)
+        *n_masked = n;
+    return HBG_OK;
+}
+
 int hbg_batch_create_blastx(const uint8_t *const *nt, const int32_t *nt_len, int32_t n_queries,
                             const int32_t *x_dropoff, const int32_t *cutoff,
                             const hbg_word_params *params, int32_t max_group_len, hbg_batch **out) {
+    return hbg_batch_create_blastx_masked(nt, nt_len, n_queries, x_dropoff, cutoff, params, nullptr,
+                                          max_group_len, out);
+}
+
+int hbg_batch_create_blastx_masked(const uint8_t *const *nt, const int32_t *nt_len, int32_t n_queries,
+                                   const int32_t *x_dropoff, const int32_t *cutoff,
+                                   const hbg_word_params *params, const hbg_seg_params *seg,
+                                   int32_t max_group_len, hbg_batch **out) {
     if (!out || !params || !nt || !nt_len || !x_dropoff || !cutoff || n_queries <= 0)
         return fail(HBG_ERR_INVALID, "hbg_batch_create_blastx: null argument or empty batch");
+    if (seg && !valid_seg(seg))
+        return fail(HBG_ERR_INVALID, "hbg_batch_create_blastx_masked: bad SEG parameters");
     *out = nullptr;
     std::vector<std::vector<uint8_t>> prot(n_queries);
     std::vector<hbg::QueryIn> qs(n_queries);
@@ -1070,6 +1103,10 @@ int hbg_batch_create_blastx(const uint8_t *const *nt, const int32_t *nt_len, int
         if ((int64_t)nt_len[k] * 2 + 6 > HBG_MAX_QUERY_LEN)
             return fail(HBG_ERR_TOO_LONG, "query " + std::to_string(k) + ": too long");
         prot[k] = hbg::translate_six_frames(nt[k], nt_len[k], &qs[k].ctx_off, &qs[k].ctx_len);
+        if (seg)                                  // each frame is masked as a protein of its own
+            for (int f = 0; f < 6; ++f)
+                hbg::seg_mask(prot[k].data() + qs[k].ctx_off[f], qs[k].ctx_len[f], seg->window, seg->locut,
+                              seg->hicut);
         qs[k].seq = prot[k].data();
         qs[k].len = qs[k].ctx_off[5] + qs[k].ctx_len[5];
         qs[k].xdrop.assign(x_dropoff + 6 * k, x_dropoff + 6 * k + 6);

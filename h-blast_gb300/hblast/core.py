@@ -49,6 +49,24 @@ class GpuOptions(C.Structure):
                 ("method", C.c_int32), ("cpu_threads", C.c_int32)]
 
 
+class SegParams(C.Structure):
+    """hbg_seg_params: SEG window and complexity cut-offs (bits)."""
+    _fields_ = [("window", C.c_int32), ("pad", C.c_int32), ("locut", C.c_double), ("hicut", C.c_double)]
+
+
+def seg_params(window: int = 12, locut: float = 2.2, hicut: float = 2.5) -> SegParams:
+    return SegParams(window, 0, locut, hicut)
+
+
+def seg_mask(seq: np.ndarray, window: int = 12, locut: float = 2.2, hicut: float = 2.5) -> np.ndarray:
+    """SEG-masked copy of an NCBIstdaa protein sequence (masked letters become X = 21)."""
+    out = np.ascontiguousarray(seq, dtype=np.uint8).copy()
+    n = C.c_int64()
+    p = seg_params(window, locut, hicut)
+    _check(lib().hbg_seg_mask(out.ctypes.data, len(out), C.byref(p), C.byref(n)))
+    return out
+
+
 class RuntimeOptions(C.Structure):
     _fields_ = [("gpu_db_used_ratio", C.c_double), ("fixed_ratio", C.c_int32), ("ccr", C.c_double),
                 ("avg_hsps_per_sequence", C.c_int32), ("mem_ecc", C.c_int32), ("balancer_method", C.c_int32),
@@ -57,10 +75,10 @@ class RuntimeOptions(C.Structure):
 
 class ServerOptions(C.Structure):
     """hbg_server_options: slots in flight, queries per batch, memory budget, group length, letters per
-    batch, shortest-first admission age."""
+    batch, shortest-first admission age, SEG masking of BLASTX frames."""
     _fields_ = [("max_inflight", C.c_int32), ("max_batch_queries", C.c_int32), ("memory_budget", C.c_int64),
                 ("max_group_len", C.c_int32), ("max_batch_letters", C.c_int32), ("shortest_first_ms", C.c_int32),
-                ("pad", C.c_int32)]
+                ("seg_blastx", C.c_int32)]
 
 
 class QueryStats(C.Structure):
@@ -87,6 +105,11 @@ _SIGS = {
     "hbg_batch_create_blastx": ([C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_int32), C.c_int32,
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(_WordParams), C.c_int32,
                                  C.POINTER(_P)], C.c_int),
+    "hbg_batch_create_blastx_masked": ([C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_int32), C.c_int32,
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(_WordParams),
+                                        C.c_void_p, C.c_int32, C.POINTER(_P)], C.c_int),
+    "hbg_seg_default_params": ([C.c_void_p], C.c_int),
+    "hbg_seg_mask": ([_P, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
     "hbg_batch_create_from_smallbone": ([C.POINTER(_Query), C.POINTER(_WordParams), _P, C.c_int32, _P,
                                          C.c_int64, C.POINTER(_P)], C.c_int),
     "hbg_batch_lookup_table": ([_P, C.c_int32, _P, _P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
@@ -285,7 +308,8 @@ class Batch:
 
     @classmethod
     def blastx(cls, nt_queries: Sequence[np.ndarray], x_dropoff: np.ndarray, cutoff: np.ndarray,
-               threshold: int = 11, window: int = 40, max_group_len: int = 0) -> "Batch":
+               threshold: int = 11, window: int = 40, max_group_len: int = 0, seg=None) -> "Batch":
+        """seg: None (no masking), True (SEG 12 2.2 2.5 on every frame) or a SegParams."""
         n = len(nt_queries)
         nts = [np.ascontiguousarray(q, dtype=np.uint8) for q in nt_queries]
         ptrs = (C.POINTER(C.c_uint8) * n)(*[q.ctypes.data_as(C.POINTER(C.c_uint8)) for q in nts])
@@ -294,8 +318,10 @@ class Batch:
         cu = np.ascontiguousarray(cutoff, dtype=np.int32).reshape(-1)
         wp = _WordParams(threshold, window)
         h = C.c_void_p()
-        _check(lib().hbg_batch_create_blastx(ptrs, _i32p(lens), n, _i32p(xd), _i32p(cu), C.byref(wp),
-                                             max_group_len, C.byref(h)))
+        sp = seg_params() if seg is True else seg
+        _check(lib().hbg_batch_create_blastx_masked(ptrs, _i32p(lens), n, _i32p(xd), _i32p(cu), C.byref(wp),
+                                                    C.byref(sp) if sp is not None else None, max_group_len,
+                                                    C.byref(h)))
         return cls(h, n)
 
     @classmethod

@@ -98,6 +98,8 @@ def parse(argv=None):
     p.add_argument("-xdrop_ungap_raw", type=int, default=16, help="ungapped X-drop in raw score units")
     p.add_argument("-cutoff_raw", type=int, default=41, help="ungapped cutoff score in raw units")
     p.add_argument("-max_batch_letters", type=int, default=8192)
+    p.add_argument("-seg", default=None, choices=["yes", "no"],
+                   help="SEG masking of BLASTX query frames (blastx default: yes; blastp queries are not masked)")
     return p.parse_args(argv)
 
 
@@ -125,8 +127,9 @@ def main(argv=None) -> int:
         for k in range(a.gpu_cards):
             opt = core.default_options(method=a.method + k, num_threadsx=a.gpu_threads, num_blocksx=a.gpu_blocks)
             db = core.Database.from_blastdb(a.db, opt)
+            seg = a.module == "blastx" and (a.seg or "yes") == "yes"
             cards.append((db, core.Server(db, a.threshold, a.window_size, opt,
-                                          max_batch_letters=a.max_batch_letters)))
+                                          max_batch_letters=a.max_batch_letters, seg_blastx=int(seg))))
         info = cards[0][0].info()
         print(f"hblastm: {a.module}, {len(queries)} queries, database {a.db}: {info[0]} sequences, "
               f"{info[1]} letters, {a.gpu_cards} card(s)", file=log)

@@ -69,6 +69,10 @@ std::vector<uint8_t> translate_six_frames(const uint8_t *nt, int32_t nt_len,
                                           std::vector<int32_t> *ctx_off,
                                           std::vector<int32_t> *ctx_len);
 
+// SEG low-complexity masking of one protein sequence in place (masked
+// letters become X); returns the number of letters masked.  seg.cpp.
+int64_t seg_mask(uint8_t *seq, int32_t len, int32_t window, double locut, double hicut);
+
 // Substitution score of NCBIstdaa letters (BLOSUM62).
 int32_t blosum62(int32_t a, int32_t b);
 const int8_t *blosum62_table();   // 28 rows x 32 columns, row = query letter

@@ -371,7 +371,7 @@ int hbg_server_default_options(hbg_server_options *o) {
     o->max_group_len = 0;
     o->max_batch_letters = 8192;
     o->shortest_first_ms = 2000;
-    o->pad = 0;
+    o->seg_blastx = 0;
     return HBG_OK;
 }
 
@@ -390,7 +390,8 @@ int hbg_server_create(hbg_db *db, const hbg_word_params *params, const hbg_gpu_o
     if (sopt)
         S->so = *sopt;
     if (S->so.max_inflight < 1 || S->so.max_inflight > 16 || S->so.max_batch_queries < 1 ||
-        S->so.memory_budget <= 0 || S->so.max_batch_letters < 0 || S->so.shortest_first_ms < 0) {
+        S->so.memory_budget <= 0 || S->so.max_batch_letters < 0 || S->so.shortest_first_ms < 0 ||
+        (S->so.seg_blastx != 0 && S->so.seg_blastx != 1)) {
         delete S;
         return HBG_ERR_INVALID;
     }
@@ -444,6 +445,9 @@ int hbg_server_submit_blastx(hbg_server *S, const uint8_t *nt, int32_t nt_len, c
         return HBG_ERR_INVALID;
     Request r;
     r.seq = hbg::translate_six_frames(nt, nt_len, &r.off, &r.len);
+    if (S->so.seg_blastx)
+        for (int f = 0; f < 6; ++f)
+            hbg::seg_mask(r.seq.data() + r.off[f], r.len[f], 12, 2.2, 2.5);
     r.xd.assign(xd, xd + 6);
     r.cu.assign(cu, cu + 6);
     return submit(S, std::move(r), ticket);

@@ -216,6 +216,34 @@ int hbg_batch_create_blastx(const uint8_t *const *nt_sequences, const int32_t *n
                             const int32_t *cutoff_score, const hbg_word_params *params,
                             int32_t max_group_len, hbg_batch **out);
 
+/* SEG low-complexity masking (NCBI's -seg option; blastx masks its
+ * translated query frames with the default "12 2.2 2.5" before the word
+ * finder runs: NF/blastx_args.cpp:133-134, query set-up at
+ * NF/blast_engine.c:367-433).  The algorithm is Wootton and Federhen's
+ * published SEG: windows of `window` letters whose compositional complexity
+ * (bits) is <= locut trigger a segment, which extends over windows <= hicut
+ * and is trimmed to its least probable subsequence; masked letters become X
+ * (hard masking). */
+typedef struct hbg_seg_params {
+    int32_t window;   /* 12 */
+    int32_t pad;
+    double locut;     /* 2.2 */
+    double hicut;     /* 2.5 */
+} hbg_seg_params;
+
+int hbg_seg_default_params(hbg_seg_params *p);
+
+/* Mask one NCBIstdaa protein sequence in place; *n_masked (may be NULL)
+ * receives the number of letters set to X. */
+int hbg_seg_mask(uint8_t *seq, int32_t len, const hbg_seg_params *p, int64_t *n_masked);
+
+/* hbg_batch_create_blastx with each translated frame SEG-masked first (seg
+ * NULL: no masking, the same as hbg_batch_create_blastx). */
+int hbg_batch_create_blastx_masked(const uint8_t *const *nt_sequences, const int32_t *nt_lengths,
+                                   int32_t n_queries, const int32_t *x_dropoff,
+                                   const int32_t *cutoff_score, const hbg_word_params *params,
+                                   const hbg_seg_params *seg, int32_t max_group_len, hbg_batch **out);
+
 /* Use a lookup table the caller already has in NCBI's small-backbone layout
  * for one query (the table H_BLAST copies at h_blast.cu:953-958):
  * backbone[i] = {num_used, payload} cells of 8 bytes (payload = 3 uint16
@@ -337,7 +365,8 @@ typedef struct hbg_server_options {
     int32_t shortest_first_ms;   /* 0: admit in arrival order.  > 0 (default 2000): requests
                                     waiting at least this long go first, in arrival order,
                                     then the shortest waiting requests */
-    int32_t pad;
+    int32_t seg_blastx;          /* 1: BLASTX requests' frames are SEG-masked with the
+                                    default parameters (blastx's own default); default 0 */
 } hbg_server_options;
 
 int hbg_server_default_options(hbg_server_options *opt);

@@ -187,3 +187,26 @@ def test_repeated_launches_replay_graph(small_db):
     ref = hblast.search(gdb, batch).hsps
     for o in outs:
         assert np.array_equal(o, ref)
+
+
+def test_blastx_seg_masked(built):
+    """BLASTX with SEG-masked frames (blastx's default query masking) against
+    the oracle run on the same frames masked by the SEG restatement."""
+    from seg_ref import seg as seg_ref
+    rng = np.random.default_rng(16)
+    prot_q = synth.random_letters(rng, 400)
+    db = synth.make_db(rng, 600, 300, 0.6, 30, 5000, 30, [prot_q], 150, 0.6)
+    nts = synth.blastx_queries(6, db, n_queries=3)
+    nts[1][60:210] = np.tile(np.array([2, 1, 3], np.uint8), 50)     # a low-complexity (Ala) run
+    xd = np.full((3, 6), 16, dtype=np.int32)
+    cu = np.full((3, 6), 41, dtype=np.int32)
+    gdb = hblast.Database(db.residues, db.offsets)
+    res = hblast.search(gdb, hblast.Batch.blastx(nts, xd, cu, seg=True))
+    pqs = []
+    for k, nt in enumerate(nts):
+        prot, off, ln = oracle.translate6(nt)
+        for f in range(6):
+            prot[off[f]:off[f] + ln[f]] = seg_ref(prot[off[f]:off[f] + ln[f]])
+        pqs.append(hblast.ProteinQuery(prot, off, ln, xd[k], cu[k]))
+    assert len(res.hsps) > 0
+    check(res, pqs, db.residues, db.offsets)

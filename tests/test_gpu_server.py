@@ -127,3 +127,17 @@ def test_search_out_of_memory_is_recoverable(served):
     s.wait()
     assert np.array_equal(s.result().hsps, ref.hsps)
     s.close()
+
+
+def test_served_blastx_with_seg(served):
+    """seg_blastx: served BLASTX requests equal a BLASTX batch built with SEG."""
+    qs, nts, db, gdb = served
+    xd6, cu6 = np.full(6, 16, np.int32), np.full(6, 41, np.int32)
+    srv = hblast.Server(gdb, max_inflight=1, max_batch_queries=4, seg_blastx=1)
+    ts = [srv.submit_blastx(nt, xd6, cu6) for nt in nts]
+    for t, nt in zip(ts, nts):
+        hsps, stats, _ = srv.take(t)
+        ref = hblast.search(gdb, hblast.Batch.blastx([nt], xd6[None], cu6[None], seg=True))
+        assert np.array_equal(hsps, ref.hsps)
+        assert stats == ref.stats[0]
+    srv.close()

@@ -36,3 +36,11 @@ def test_no_cpu_path_and_card_checks(tmp_path, built):
     assert "no CPU path" in log.read_text()
     assert hblastm.main(["-query", str(q), "-db", "x", "-gpu_cards", "64", "-screen_out", str(log)]) == 2
     assert "visible GPU" in log.read_text()
+
+
+def test_seg_option():
+    a = hblastm.parse(["-query", "q", "-db", "d", "-module", "blastx"])
+    assert a.seg is None                       # blastx default: masked (resolved to yes)
+    assert hblastm.parse(["-query", "q", "-db", "d", "-seg", "no"]).seg == "no"
+    with pytest.raises(SystemExit):
+        hblastm.parse(["-query", "q", "-db", "d", "-seg", "maybe"])
