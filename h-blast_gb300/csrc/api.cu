@@ -180,6 +180,7 @@ struct LaunchClass {
 struct LaunchShape {
     int threads;
     int blocks;
+    int team;        // groups per tile (warps that share each subject)
 };
 constexpr int kMaxLaunchClasses = 32;
 
@@ -215,6 +216,8 @@ struct hbg_batch {
     std::vector<LaunchClass> classes;
     int64_t device_bytes = 0;
     int32_t tile_subjects = 0;   // 0 = automatic (hbg_batch_tune)
+    int64_t tile_bytes = 0;      // > 0: tiles of about this many subject letters (hbg_batch_schedule)
+    int32_t team = 1;            // groups searched together per pass over a subject (hbg_batch_schedule)
 };
 
 struct hbg_result {
@@ -365,6 +368,10 @@ int32_t global_diag_len(const hbg::HostBatch &h, const hbg_db *db) {
 int32_t class_tile_subjects(const hbg_batch *b, const hbg_db *db, const LaunchClass &lc, int blocks) {
     if (b->tile_subjects > 0)
         return b->tile_subjects;
+    if (b->tile_bytes > 0) {                  // subjects of the database's mean length
+        const int64_t mean = std::max<int64_t>(1, db->n_res / std::max<int32_t>(1, db->n));
+        return (int32_t)std::max<int64_t>(1, std::min<int64_t>(1 << 20, b->tile_bytes / mean));
+    }
     const int64_t want = (int64_t)db->n * lc.count / (8 * (int64_t)std::max(blocks, 1));
     return (int32_t)std::max<int64_t>(8, std::min<int64_t>(128, want));
 }
@@ -381,12 +388,17 @@ int plan_launches(const hbg_batch *b, const hbg_gpu_options &o, int device, std:
         // num_threadsx is the largest CTA size: per class take the size (halving
         // down to 64) that keeps the most warps resident per SM -- large diagonal
         // tables fill shared memory, and smaller CTAs pack it better
+        // with several groups per pass (team > 1) the CTA keeps at least one
+        // warp per group
         int best_t = 0, best_per = 0, best_warps = -1;
         for (int t = o.num_threadsx; t >= 32; t = t > 64 ? ((t / 2) + 31) / 32 * 32 : 0) {
-            if (hbg::wordfinder_smem_bytes(t, lc.smem_diag) > (size_t)optin)
+            const int team = std::min(b->team, t / 32);
+            if (team < b->team && best_t > 0)
+                break;
+            if (hbg::wordfinder_smem_bytes(t, lc.smem_diag, team) > (size_t)optin)
                 continue;
             int per = 0;
-            if (hbg::wordfinder_occupancy(lc.mode, t, lc.smem_diag, &per) != cudaSuccess || per < 1)
+            if (hbg::wordfinder_occupancy(lc.mode, t, lc.smem_diag, team, &per) != cudaSuccess || per < 1)
                 per = 1;
             if (per * (t / 32) > best_warps) {
                 best_t = t;
@@ -399,7 +411,7 @@ int plan_launches(const hbg_batch *b, const hbg_gpu_options &o, int device, std:
         if (best_t == 0)
             return fail(HBG_ERR_TOO_LONG, "group diagonal tables exceed shared memory");
         const int blocks = o.num_blocksx > 0 ? o.num_blocksx : sms * best_per;
-        out->push_back(LaunchShape{best_t, blocks});
+        out->push_back(LaunchShape{best_t, blocks, std::min(b->team, best_t / 32)});
     }
     return HBG_OK;
 }
@@ -545,8 +557,10 @@ int enqueue_search(hbg_result *r) {
             const LaunchClass &lc = b->classes[c];
             a.tile_subjects = class_tile_subjects(b, db, lc, r->shapes[c].blocks);
             a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
+            a.team = r->shapes[c].team;
+            a.n_list = lc.count;
             a.group_list = b->d_group_list + lc.first;
-            a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
+            a.n_tiles = (int64_t)a.tiles_per_group * ((lc.count + a.team - 1) / a.team);
             a.tile_counter = r->d_tile + c;
             a.smem_diag = lc.smem_diag;
             CU(hbg::launch_wordfinder(a, lc.mode, r->shapes[c].blocks, r->shapes[c].threads, st));
@@ -1243,6 +1257,17 @@ int hbg_batch_tune(hbg_batch *b, int32_t tile_subjects, int32_t global_tables) {
     return HBG_OK;
 }
 
+int hbg_batch_schedule(hbg_batch *b, int32_t warps_per_subject, int64_t tile_bytes) {
+    if (!b || warps_per_subject < 1 || warps_per_subject > 8 || tile_bytes < 0 ||
+        (tile_bytes > 0 && (tile_bytes < 1024 || tile_bytes > ((int64_t)1 << 24))))
+        return fail(HBG_ERR_INVALID, "hbg_batch_schedule: warps_per_subject 1..8, tile_bytes 0 or 1 KiB..16 MiB");
+    if (b->device >= 0)
+        return fail(HBG_ERR_STATE, "batch already uploaded: schedule before the first search");
+    b->team = warps_per_subject;
+    b->tile_bytes = tile_bytes;
+    return HBG_OK;
+}
+
 int hbg_batch_destroy(hbg_batch *b) {
     if (!b)
         return fail(HBG_ERR_INVALID, "null batch");
@@ -1656,8 +1681,10 @@ extern "C" int hbg_search_static(const hbg_db *db, const hbg_batch *batch, const
             const LaunchClass &lc = batch->classes[c];
             a.tile_subjects = class_tile_subjects(batch, db, lc, shapes[c].blocks);
             a.tiles_per_group = (db->n + a.tile_subjects - 1) / a.tile_subjects;
+            a.team = shapes[c].team;
+            a.n_list = lc.count;
             a.group_list = batch->d_group_list + lc.first;
-            a.n_tiles = (int64_t)a.tiles_per_group * lc.count;
+            a.n_tiles = (int64_t)a.tiles_per_group * ((lc.count + a.team - 1) / a.team);
             a.tile_counter = tile + c;
             a.smem_diag = lc.smem_diag;
             CU(hbg::launch_wordfinder(a, lc.mode, shapes[c].blocks, shapes[c].threads, st));

@@ -28,11 +28,15 @@ struct WordFinderArgs {
     const HbgContext *contexts;
     const HbgQueryDesc *queries;
     int32_t window;
-    // scheduling: tile t covers group group_list[t / tiles_per_group] and
-    // scheduled subjects [(t % tiles_per_group) * tile_subjects, + tile_subjects)
+    // scheduling: tile t covers groups group_list[(t / tiles_per_group) * team
+    // .. + team) (those below n_list) and scheduled subjects
+    // [(t % tiles_per_group) * tile_subjects, + tile_subjects); warp w of a
+    // CTA works on the tile's group w % team
     int32_t tile_subjects;
     int32_t tiles_per_group;
     int64_t n_tiles;
+    int32_t team;                 // groups per tile: warps that share each subject, 1..warps per CTA
+    int32_t n_list;               // groups in group_list
     unsigned int *tile_counter;   // zeroed before launch
     // outputs
     hbg_hsp *hsps;
@@ -50,11 +54,13 @@ struct WordFinderArgs {
 };
 
 // Shared memory the word-finder kernel needs for a CTA of `threads` threads.
-size_t wordfinder_smem_bytes(int threads, int smem_diag);
+size_t wordfinder_smem_bytes(int threads, int smem_diag, int team);
 cudaError_t wordfinder_configure();
 // mode: bit 0 = offset mode (else chunk mode); bit 1 = the groups keep
-// their diagonal tables in global memory (kernel built to favour L1)
-cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm);
+// their diagonal tables in global memory (kernel built to favour L1); the
+// instantiation for tiles of several groups (team > 1) is chosen from
+// WordFinderArgs::team / the team argument
+cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int team, int *blocks_per_sm);
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream);
 

@@ -39,16 +39,29 @@ __constant__ int8_t c_blosum[28 * 32] = {
 #include "blosum62.inc"
 };
 
-struct __align__(16) Smem {   // 16-byte size: the per-warp tables after it are cleared with 16-byte stores
-    uint32_t pv[HBG_PV_WORDS];
-    int8_t matrix[28 * 32];
-    unsigned int q_ext[kMaxQ];
-    unsigned int q_kept[kMaxQ];
-    unsigned long long hits;
+// Dynamic shared memory of a CTA: a Head, then one Slot per query group the
+// CTA searches at a time (the groups that share each pass over a block of
+// subjects: "warps per subject"), then the per-warp regions and tables.
+// Sizes are multiples of 16 bytes: the per-warp tables after them are
+// cleared with 16-byte stores.
+extern __shared__ __align__(16) unsigned char g_smem[];
+
+struct __align__(16) Head {
+    int8_t matrix[28 * 32];   // BLOSUM62, query letter x 32 + subject letter
     long long tile;
-    int next;
-    int pad;
+    long long pad;
 };
+
+struct __align__(16) Slot {
+    uint32_t pv[HBG_PV_WORDS];   // presence vector of the slot's group
+    unsigned int q_ext[kMaxQ];   // per query of the group: extensions tried, kept
+    unsigned int q_kept[kMaxQ];
+    unsigned long long hits;     // lookup hits of the group in this tile
+    int next;                    // next subject of the tile for the slot's warps
+    int group;                   // group index, -1 when the tile has none for this slot
+};
+
+__device__ __forceinline__ const int8_t *score_matrix() { return reinterpret_cast<const Head *>(g_smem)->matrix; }
 
 __device__ __forceinline__ int sc(const int8_t *m, int q, int s) { return m[q * 32 + s]; }
 
@@ -232,8 +245,8 @@ struct WarpQueue {
     int blk_s[2][kQueue];
     int blk_q[2][kQueue];
 };
-// the 16-bit tables follow Smem and the queues and are cleared 16 bytes at a time
-static_assert(sizeof(Smem) % 16 == 0 && sizeof(WarpQueue) % 16 == 0,
+// the 16-bit tables follow the head, the slots and the queues and are cleared 16 bytes at a time
+static_assert(sizeof(Head) % 16 == 0 && sizeof(Slot) % 16 == 0 && sizeof(WarpQueue) % 16 == 0,
               "shared-memory regions must keep 16-byte alignment (table lengths are multiples of 8)");
 
 template <typename Cell>
@@ -345,7 +358,7 @@ __device__ __forceinline__ void apply_hits(const Item<Cell> &it, bool act, int d
 // wait.  With drain, run everything and repeat until both lists are empty
 // (needed before the subject ends).  Warp-collective.
 template <typename Cell>
-__device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, WarpQueue &wq,
+__device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Slot &sh, WarpQueue &wq,
                       int &n_tasks, int &n_blk, int &blk_cur, bool drain) {
     using T = CellTraits<Cell>;
     const int lane = threadIdx.x & 31;
@@ -359,7 +372,7 @@ __device__ void flush(const Item<Cell> &it, const WordFinderArgs &a, Smem &sh, W
                 const HbgContext C = a.contexts[ci];
                 const HbgQueryDesc Q = a.queries[C.query];
                 const int ql = q - Q.start;
-                const Ext e = extend_two_hit(sh.matrix, it.s, it.S, it.gseq + Q.start, Q.len,
+                const Ext e = extend_two_hit(score_matrix(), it.s, it.S, it.gseq + Q.start, Q.len,
                                              wq.task_left[i], s_h, ql, C.x_dropoff);
                 atomicAdd(&sh.q_ext[C.query - it.first_query], 1u);
                 if (e.score >= C.cutoff) {
@@ -496,7 +509,7 @@ __device__ __forceinline__ void stage_end() {
 // presence test and cell bounds: *c = hits of that offset, *base = first
 // entry.  Warp-collective.
 template <typename Cell>
-__device__ __forceinline__ void scan_words(const Item<Cell> &it, Stage &stg, WarpQueue &wq, const Smem &sh,
+__device__ __forceinline__ void scan_words(const Item<Cell> &it, Stage &stg, WarpQueue &wq, const Slot &sh,
                                            const uint32_t *cs, int s0, uint32_t *c, uint32_t *base) {
     const int lane = threadIdx.x & 31;
     // the words of this chunk need letters up to delta + s0 + 33
@@ -522,7 +535,7 @@ __device__ __forceinline__ void scan_words(const Item<Cell> &it, Stage &stg, War
 // offsets at a time, the hits of the chunk compacted in CPU order and applied
 // 32 at a time.  Warp-collective.
 template <typename Cell>
-__device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
+__device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Slot &sh,
                                            WarpQueue &wq, const uint32_t *cs, const uint16_t *ents,
                                            int diag_alloc) {
     const int lane = threadIdx.x & 31;
@@ -632,7 +645,7 @@ __device__ __forceinline__ void apply_offset(const Item<Cell> &it, bool act, int
 }
 
 template <typename Cell>
-__device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFinderArgs &a, Smem &sh,
+__device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFinderArgs &a, Slot &sh,
                                                    WarpQueue &wq, const uint32_t *cs,
                                                    const uint16_t *ents, int diag_alloc) {
     const int lane = threadIdx.x & 31;
@@ -690,24 +703,33 @@ __device__ unsigned long long process_item_offsets(Item<Cell> &it, const WordFin
 // Mode bit 0: offset mode (else chunk mode); bit 1: the launch's groups keep
 // their diagonal tables in global memory (same code; that instantiation asks
 // for a small shared-memory carve-out so the L1 cache holds more of the
-// tables).  Chunk mode is built for four 256-thread CTAs per SM (64
-// registers a thread), offset mode (large tables) for one.
+// tables); bit 2: tiles of several groups (warps per subject > 1).  Chunk
+// mode is built for four 256-thread CTAs per SM (64 registers a thread),
+// offset mode (large tables) for one.
 template <int Mode>
 __global__ void __launch_bounds__(256, (Mode & 1) == 0 ? 4 : 1) wordfinder_kernel(WordFinderArgs a) {
     constexpr bool kOffsets = (Mode & 1) != 0;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem &sh = *reinterpret_cast<Smem *>(smem_raw);
+    constexpr bool kTeam = (Mode & 4) != 0;   // several groups per tile (built apart: it needs more registers)
+    Head &hd = *reinterpret_cast<Head *>(g_smem);
+    Slot *slots = reinterpret_cast<Slot *>(g_smem + sizeof(Head));
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
-    WarpQueue &wq = reinterpret_cast<WarpQueue *>(smem_raw + sizeof(Smem))[warp];
+    // a tile covers `team` groups and one block of subjects; warp w serves
+    // group slot w % team, and the warps of a slot share its subjects
+    const int team = kTeam ? a.team : 1;
+    Slot &sh = slots[warp % team];
+    unsigned char *per_warp = g_smem + sizeof(Head) + (size_t)team * sizeof(Slot);
+    WarpQueue &wq = reinterpret_cast<WarpQueue *>(per_warp)[warp];
     uint16_t *diag_s =
-        reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem) + nwarps * sizeof(WarpQueue)) + warp * a.smem_diag;
+        reinterpret_cast<uint16_t *>(per_warp + nwarps * sizeof(WarpQueue)) + warp * a.smem_diag;
     uint32_t *diag_g =
         a.gdiag ? a.gdiag + ((size_t)blockIdx.x * nwarps + warp) * (size_t)a.gdiag_len : nullptr;
 
     for (int i = threadIdx.x; i < 28 * 32; i += blockDim.x)
-        sh.matrix[i] = c_blosum[i];
+        hd.matrix[i] = c_blosum[i];
+    for (int i = threadIdx.x; i < team; i += blockDim.x)
+        slots[i].group = -1;
     for (int i = lane; i < a.smem_diag; i += 32)
         diag_s[i] = 0;
     const int window = a.window;
@@ -717,91 +739,126 @@ __global__ void __launch_bounds__(256, (Mode & 1) == 0 ? 4 : 1) wordfinder_kerne
     // forces the other view to clear before its next use)
     int32_t dofs_s = CellTraits<uint16_t>::kLimit + 1, dofs_g = window;
     int32_t dofs_h = CellTraits<uint16_t>::kLimit + 1;
-    int cur_group = -1;
 
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) {
-            sh.tile = (long long)atomicAdd(a.tile_counter, 1u);
-            sh.next = 0;
-            sh.hits = 0;
+        if (threadIdx.x == 0)
+            hd.tile = (long long)atomicAdd(a.tile_counter, 1u);
+        for (int i = threadIdx.x; i < team * kMaxQ; i += blockDim.x) {
+            slots[i / kMaxQ].q_ext[i % kMaxQ] = 0;
+            slots[i / kMaxQ].q_kept[i % kMaxQ] = 0;
         }
-        for (int i = threadIdx.x; i < kMaxQ; i += blockDim.x) {
-            sh.q_ext[i] = 0;
-            sh.q_kept[i] = 0;
+        for (int i = threadIdx.x; i < team; i += blockDim.x) {
+            slots[i].next = 0;
+            slots[i].hits = 0;
         }
         __syncthreads();
-        const long long tile = sh.tile;
+        const long long tile = hd.tile;
         if (tile >= a.n_tiles)
             break;
-        const int g = a.group_list[tile / a.tiles_per_group];
+        const long long gb = tile / a.tiles_per_group;
         const int blk = (int)(tile % a.tiles_per_group);
-        if (g != cur_group) {
-            const uint32_t *src = a.pv + (size_t)g * HBG_PV_WORDS;
-            for (int i = threadIdx.x; i < HBG_PV_WORDS; i += blockDim.x)
-                sh.pv[i] = src[i];
-            cur_group = g;
-            __syncthreads();
-        }
-        const HbgGroup G = a.groups[g];
-        const uint32_t *cs = a.cells + (size_t)g * HBG_CELL_STRIDE;
-        const uint16_t *ents = a.entries + G.entry_base;
-
-        for (;;) {
-            int k = 0;
-            if (lane == 0)
-                k = atomicAdd(&sh.next, 1);
-            k = __shfl_sync(0xffffffffu, k, 0);
-            const long long idx = (long long)blk * a.tile_subjects + k;
-            if (k >= a.tile_subjects || idx >= a.n_subj)
-                break;
-            const int j = a.order[idx];
-            const int S = a.db_len[j];
-            const uint8_t *sp = a.db + a.db_off[j];
-            unsigned long long hits;
-            // 16-bit cells when window + S fits 15 bits: in shared memory when the
-            // group's table fits there, else in this warp's slice of the global
-            // scratch (half the footprint of 32-bit cells, so the tables of all
-            // resident warps stay in L2); otherwise 32-bit cells in that slice
-            if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
-                Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
-                                  a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
-                                : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
-                dofs_s = it.dofs;
-            } else if (window + S <= CellTraits<uint16_t>::kLimit) {
-                Item<uint16_t> it{sp, S, j, reinterpret_cast<uint16_t *>(diag_g), G.diag_len - 1, dofs_h,
-                                  window, a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, 2 * a.gdiag_len)
-                                : process_item(it, a, sh, wq, cs, ents, 2 * a.gdiag_len);
-                dofs_h = it.dofs;
-                dofs_g = kWrap32;                  // the 32-bit view clears before its next use
-            } else {
-                Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
-                                  a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
-                hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
-                                : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
-                dofs_g = it.dofs;
-                dofs_h = CellTraits<uint16_t>::kLimit + 1;   // the 16-bit view clears before its next use
+        // the presence vectors of this tile's groups (kept when a slot keeps its group)
+        for (int t = 0; t < team; ++t) {
+            const long long li = gb * team + t;
+            const int g = li < a.n_list ? a.group_list[li] : -1;
+            if (g >= 0 && g != slots[t].group) {
+                const uint32_t *src = a.pv + (size_t)g * HBG_PV_WORDS;
+                for (int i = threadIdx.x; i < HBG_PV_WORDS; i += blockDim.x)
+                    slots[t].pv[i] = src[i];
             }
-            if (lane == 0)
-                atomicAdd(&sh.hits, hits);
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < G.n_queries && i < kMaxQ; i += blockDim.x) {
-            if (sh.q_ext[i])
-                atomicAdd(a.q_extended + G.first_query + i, (unsigned long long)sh.q_ext[i]);
-            if (sh.q_kept[i])
-                atomicAdd(a.q_kept + G.first_query + i, (unsigned long long)sh.q_kept[i]);
+        if (threadIdx.x < team) {
+            const long long li = gb * team + threadIdx.x;
+            slots[threadIdx.x].group = li < a.n_list ? a.group_list[li] : -1;
         }
-        if (threadIdx.x == 0 && sh.hits)
-            atomicAdd(a.g_hits + g, sh.hits);
+        __syncthreads();
+        const int g = sh.group;
+        if (g >= 0) {
+            const HbgGroup G = a.groups[g];
+            const uint32_t *cs = a.cells + (size_t)g * HBG_CELL_STRIDE;
+            const uint16_t *ents = a.entries + G.entry_base;
+            for (;;) {
+                int k = 0;
+                if (lane == 0)
+                    k = atomicAdd(&sh.next, 1);
+                k = __shfl_sync(0xffffffffu, k, 0);
+                const long long idx = (long long)blk * a.tile_subjects + k;
+                if (k >= a.tile_subjects || idx >= a.n_subj)
+                    break;
+                const int j = a.order[idx];
+                const int S = a.db_len[j];
+                const uint8_t *sp = a.db + a.db_off[j];
+                unsigned long long hits;
+                // 16-bit cells when window + S fits 15 bits: in shared memory when the
+                // group's table fits there, else in this warp's slice of the global
+                // scratch (half the footprint of 32-bit cells, so the tables of all
+                // resident warps stay in L2); otherwise 32-bit cells in that slice
+                if (!G.placement && window + S <= CellTraits<uint16_t>::kLimit) {
+                    Item<uint16_t> it{sp, S, j, diag_s, G.diag_len - 1, dofs_s, window,
+                                      a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
+                    hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.smem_diag)
+                                    : process_item(it, a, sh, wq, cs, ents, a.smem_diag);
+                    dofs_s = it.dofs;
+                } else if (window + S <= CellTraits<uint16_t>::kLimit) {
+                    Item<uint16_t> it{sp, S, j, reinterpret_cast<uint16_t *>(diag_g), G.diag_len - 1, dofs_h,
+                                      window, a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
+                    hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, 2 * a.gdiag_len)
+                                    : process_item(it, a, sh, wq, cs, ents, 2 * a.gdiag_len);
+                    dofs_h = it.dofs;
+                    dofs_g = kWrap32;                  // the 32-bit view clears before its next use
+                } else {
+                    Item<uint32_t> it{sp, S, j, diag_g, G.diag_len - 1, dofs_g, window,
+                                      a.letters + G.seq_base, a.ctx_of + G.seq_base, G.first_query};
+                    hits = kOffsets ? process_item_offsets(it, a, sh, wq, cs, ents, a.gdiag_len)
+                                    : process_item(it, a, sh, wq, cs, ents, a.gdiag_len);
+                    dofs_g = it.dofs;
+                    dofs_h = CellTraits<uint16_t>::kLimit + 1;   // the 16-bit view clears before its next use
+                }
+                if (lane == 0)
+                    atomicAdd(&sh.hits, hits);
+            }
+        }
+        __syncthreads();
+        for (int t = 0; t < team; ++t) {
+            const int gt = slots[t].group;
+            if (gt < 0)
+                continue;
+            const HbgGroup Gt = a.groups[gt];
+            for (int i = threadIdx.x; i < Gt.n_queries && i < kMaxQ; i += blockDim.x) {
+                if (slots[t].q_ext[i])
+                    atomicAdd(a.q_extended + Gt.first_query + i, (unsigned long long)slots[t].q_ext[i]);
+                if (slots[t].q_kept[i])
+                    atomicAdd(a.q_kept + Gt.first_query + i, (unsigned long long)slots[t].q_kept[i]);
+            }
+            if (threadIdx.x == 0 && slots[t].hits)
+                atomicAdd(a.g_hits + gt, slots[t].hits);
+        }
     }
 }
 
-size_t wordfinder_smem_bytes(int threads, int smem_diag) {
-    return sizeof(Smem) + (size_t)(threads / 32) * (sizeof(WarpQueue) + (size_t)smem_diag * sizeof(uint16_t));
+size_t wordfinder_smem_bytes(int threads, int smem_diag, int team) {
+    return sizeof(Head) + (size_t)team * sizeof(Slot) +
+           (size_t)(threads / 32) * (sizeof(WarpQueue) + (size_t)smem_diag * sizeof(uint16_t));
 }
+
+namespace {
+template <int M>
+const void *kernel_ptr() { return (const void *)wordfinder_kernel<M>; }
+const void *kernel_of(int mode) {
+    switch (mode & 7) {
+    case 0: return kernel_ptr<0>();
+    case 1: return kernel_ptr<1>();
+    case 2: return kernel_ptr<2>();
+    case 3: return kernel_ptr<3>();
+    case 4: return kernel_ptr<4>();
+    case 5: return kernel_ptr<5>();
+    case 6: return kernel_ptr<6>();
+    default: return kernel_ptr<7>();
+    }
+}
+}  // namespace
 
 cudaError_t wordfinder_configure() {
     // opt in to the largest shared-memory carve-out; launches size their own.
@@ -812,36 +869,34 @@ cudaError_t wordfinder_configure() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const void *k[4] = {(const void *)wordfinder_kernel<0>, (const void *)wordfinder_kernel<1>,
-                        (const void *)wordfinder_kernel<2>, (const void *)wordfinder_kernel<3>};
-    for (int m = 0; m < 4; ++m) {
-        cudaError_t e = cudaFuncSetAttribute(k[m], cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    for (int m = 0; m < 8; ++m) {
+        cudaError_t e = cudaFuncSetAttribute(kernel_of(m), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         if (e == cudaSuccess && (m & 2))
-            e = cudaFuncSetAttribute(k[m], cudaFuncAttributePreferredSharedMemoryCarveout, 40);
+            e = cudaFuncSetAttribute(kernel_of(m), cudaFuncAttributePreferredSharedMemoryCarveout, 40);
         if (e != cudaSuccess)
             return e;
     }
     return cudaSuccess;
 }
 
-cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int *blocks_per_sm) {
-    const size_t smem = wordfinder_smem_bytes(threads, smem_diag);
-    switch (mode & 3) {
-    case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<0>, threads, smem);
-    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<1>, threads, smem);
-    case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<2>, threads, smem);
-    default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wordfinder_kernel<3>, threads, smem);
-    }
+cudaError_t wordfinder_occupancy(int mode, int threads, int smem_diag, int team, int *blocks_per_sm) {
+    const size_t smem = wordfinder_smem_bytes(threads, smem_diag, team);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel_of((mode & 3) | (team > 1 ? 4 : 0)),
+                                                         threads, smem);
 }
 
 cudaError_t launch_wordfinder(const WordFinderArgs &a, int mode, int blocks, int threads,
                               cudaStream_t stream) {
-    const size_t smem = wordfinder_smem_bytes(threads, a.smem_diag);
-    switch (mode & 3) {
+    const size_t smem = wordfinder_smem_bytes(threads, a.smem_diag, a.team);
+    switch ((mode & 3) | (a.team > 1 ? 4 : 0)) {
     case 0: wordfinder_kernel<0><<<blocks, threads, smem, stream>>>(a); break;
     case 1: wordfinder_kernel<1><<<blocks, threads, smem, stream>>>(a); break;
     case 2: wordfinder_kernel<2><<<blocks, threads, smem, stream>>>(a); break;
-    default: wordfinder_kernel<3><<<blocks, threads, smem, stream>>>(a); break;
+    case 3: wordfinder_kernel<3><<<blocks, threads, smem, stream>>>(a); break;
+    case 4: wordfinder_kernel<4><<<blocks, threads, smem, stream>>>(a); break;
+    case 5: wordfinder_kernel<5><<<blocks, threads, smem, stream>>>(a); break;
+    case 6: wordfinder_kernel<6><<<blocks, threads, smem, stream>>>(a); break;
+    default: wordfinder_kernel<7><<<blocks, threads, smem, stream>>>(a); break;
     }
     return cudaGetLastError();
 }

@@ -115,6 +115,7 @@ _SIGS = {
     "hbg_batch_lookup_table": ([_P, C.c_int32, _P, _P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), _P], C.c_int),
     "hbg_batch_set_mode": ([_P, C.c_int32, C.c_int32], C.c_int),
+    "hbg_batch_schedule": ([_P, C.c_int32, C.c_int64], C.c_int),
     "hbg_batch_destroy": ([_P], C.c_int),
     "hbg_batch_info": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
                         C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
@@ -364,6 +365,12 @@ class Batch:
     def tune(self, tile_subjects: int = 0, global_tables: bool = False) -> "Batch":
         """hbg_batch_tune: subjects per work unit (0 = automatic), diagonal tables in global memory."""
         _check(lib().hbg_batch_tune(self.handle, tile_subjects, int(global_tables)))
+        return self
+
+    def schedule(self, warps_per_subject: int = 1, tile_bytes: int = 0) -> "Batch":
+        """Groups sharing each pass over a subject, and work-unit size in subject letters (before the
+        first search)."""
+        _check(lib().hbg_batch_schedule(self.handle, warps_per_subject, tile_bytes))
         return self
 
     def set_mode(self, mode: int, group: int = -1) -> "Batch":

@@ -283,6 +283,20 @@ int hbg_batch_set_mode(hbg_batch *batch, int32_t g, int32_t mode);
  * arrays are global, h_blast_kernel.cu:603-630.) */
 int hbg_batch_tune(hbg_batch *batch, int32_t tile_subjects, int32_t global_tables);
 
+/* Scheduling knobs for tuning (results do not depend on them).
+ * warps_per_subject (1..8): how many query groups share each pass over a
+ * block of subjects.  1 (default): the warps of a CTA take different subjects
+ * of one group.  W > 1: a CTA searches W groups at a time, warp w serving
+ * group w mod W, so W warps (up to the whole CTA) read each subject and its
+ * letters come from the SM's caches after the first.  tile_bytes (0 =
+ * automatic, else 1 KiB..16 MiB): subjects per work unit sized by letters,
+ * about tile_bytes / mean subject length (hbg_batch_tune's tile_subjects,
+ * when set, wins).  H-BLAST fixes the corresponding choices at compile time
+ * or by query length: one thread per subject (kernel K-A,
+ * h_blast_kernel.cu:504) or four (K-B, :21), chosen at
+ * NF/functions.cpp:1400-1406.  Call before the batch's first search. */
+int hbg_batch_schedule(hbg_batch *batch, int32_t warps_per_subject, int64_t tile_bytes);
+
 int hbg_batch_destroy(hbg_batch *batch);
 /* Sizes of a batch; device_bytes is what its upload copies host-to-device. */
 int hbg_batch_info(const hbg_batch *batch, int32_t *n_queries, int32_t *n_groups,

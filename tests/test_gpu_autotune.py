@@ -45,3 +45,24 @@ def test_tuning_knobs_keep_results(built):
         assert r.stats == ref.stats
     with pytest.raises(hblast.HblastError):
         hblast.Batch.proteins(pqs).tune(5, False)
+
+
+def test_schedule_knobs_keep_results(built):
+    """Warps per subject (groups sharing each pass over a subject, up to one
+    CTA) and work units sized in subject bytes change no HSP or counter."""
+    rng = np.random.default_rng(57)
+    qs = [synth.random_letters(rng, int(n)) for n in rng.integers(40, 1500, size=40)] + \
+         [synth.random_letters(rng, 3000), synth.random_letters(rng, 40000 // 10)]
+    db = synth.make_db(rng, 3000, 300, 0.6, 30, 5000, 0.05, qs, lambda r: r.integers(50, 301), 0.5)
+    gdb = hblast.Database(db.residues, db.offsets)
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    for glen in (0, 2008):
+        ref = hblast.search(gdb, hblast.Batch.proteins(pqs, max_group_len=glen))
+        assert hblast.Batch.proteins(pqs, max_group_len=glen).info()["n_groups"] > 8
+        for team, tb in ((2, 0), (3, 0), (8, 0), (1, 4096), (1, 65536), (8, 16384), (4, 1024)):
+            r = hblast.search(gdb, hblast.Batch.proteins(pqs, max_group_len=glen).schedule(team, tb))
+            assert np.array_equal(r.hsps, ref.hsps), (glen, team, tb)
+            assert r.stats == ref.stats, (glen, team, tb)
+    for bad in ((0, 0), (9, 0), (1, 100), (1, 1 << 25)):
+        with pytest.raises(hblast.HblastError):
+            hblast.Batch.proteins(pqs).schedule(*bad)

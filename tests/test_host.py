@@ -206,3 +206,12 @@ def test_allocation_failure_hook_validates(built):
         hblast.fail_allocations(-1)
     hblast.fail_allocations(2)
     hblast.fail_allocations(0)
+
+
+def test_schedule_validates_before_upload(built):
+    b = hblast.Batch.proteins([hblast.ProteinQuery.blastp(np.ones(50, np.uint8) * 3)])
+    b.schedule(4, 8192).schedule(1, 0)
+    for bad in ((0, 0), (9, 0), (2, 512), (2, -1)):
+        with pytest.raises(hblast.HblastError):
+            b.schedule(*bad)
+    b.close()
