@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--rates", default="50,200,1000,2000", help="served: Poisson arrival rates (queries/s)")
     p.add_argument("--requests", type=int, default=1000, help="served: requests per rate")
     p.add_argument("--forms", default="served,plain", help="served: forms to run (served, served_2, served_fifo, plain)")
+    p.add_argument("--batches", default="1,8,64", help="autotune: query batch sizes")
     p.add_argument("--subjects", type=int, default=0, help="override the database size (testing)")
     p.add_argument("--queries", type=int, default=0, help="override the number of queries (testing)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
@@ -303,23 +304,22 @@ def served_arm(args):
 
 
 def autotune_arm(args):
-    """Config-4 sweep: batches of 1, 8, 64 and 512 heavy-tailed queries (lognormal median 350,
-    sigma 1.0, 30..35,000 aa) against a database sample; per length bucket the tuner's choice and
-    the achieved subject-stream GB/s of every candidate."""
+    """Config-4 sweep: batches (default 1, 8 and 64; --batches) of heavy-tailed queries (lognormal
+    median 350, sigma 1.0, 30..35,000 aa) against the 10,000,000-subject database (--subjects for a
+    sample); per length bucket the tuner's choice and the achieved subject-stream GB/s of every
+    candidate."""
     import torch
     torch.cuda.set_device(0)
     import __graft_entry__ as g
     g.build()
     import hblast
     from hblast import autotune, synth
-    n_sub = args.subjects or 500_000
-    rng = np.random.default_rng(0)
-    db = synth.make_db(rng, n_sub, 300, 0.6, 30, 5000, 0.01, [synth.random_letters(rng, 400)],
-                       lambda r: r.integers(50, 301), lambda r: r.uniform(0.3, 0.6))
+    n_sub = args.subjects or 10_000_000
+    db = synth.large_db(0, n_sub)
     gdb = hblast.Database(db.residues, db.offsets)
     ssum = int(db.offsets[-1])
     report = {"metric": "autotune", "config": {"workload": f"heavy-tailed batches vs {n_sub} subjects ({ssum} residues)"}}
-    for nb in (1, 8, 64, 512):
+    for nb in (int(x) for x in args.batches.split(",")):
         qs = synth.heavy_tailed_queries(nb, nb)
         pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
         table = autotune.tune(gdb, pqs, ssum, reps=1)

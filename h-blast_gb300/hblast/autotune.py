@@ -1,10 +1,13 @@
 """Autotuner for the word finder: per query-length bucket, choose the query
 group length, the hit mode (chunk mode / offset mode), the CTA size, the
-subjects per work unit (the subject chunk a CTA takes: 32, 128 or 512
-subjects, about 11, 46 or 184 KB of letters) and the diagonal-table placement
-(shared or global memory) by timing searches of the bucket's queries against
-a sample of the database.  Stage one times the group-length / mode / CTA
-candidates; stage two varies the work unit and the placement of the best.
+subject chunk a CTA takes (by count: 32, 128 or 512 subjects, about 11, 46 or
+184 KB of letters; or by bytes: 4, 16 or 64 KB of subject letters), the
+threads per subject (one warp; or 2, 4, 8 warps: that many query groups share
+each pass over a subject, 8 warps being one CTA per subject) and the
+diagonal-table placement (shared or global memory) by timing searches of the
+bucket's queries against the database.  Stage one times the group-length /
+mode / CTA candidates; stage two varies the chunk, the threads per subject
+and the placement of the best.
 
 Every choice gives identical HSPs (the tests check it); only time changes.
 The report lists, per bucket and candidate, the word-finder time, the
@@ -33,13 +36,17 @@ class Choice:
     threads: int            # largest CTA size
     tile_subjects: int = 0  # subjects per work unit, 0 = automatic
     global_tables: bool = False
+    warps_per_subject: int = 1  # query groups sharing each pass over a subject
+    tile_bytes: int = 0     # work unit by subject letters, 0 = automatic
 
 
 DEFAULT_CANDIDATES = (
     Choice(1, 0, 256), Choice(1000, 0, 256), Choice(2008, 0, 256), Choice(4056, 0, 256),
     Choice(6000, 0, 256), Choice(8152, 1, 256), Choice(16344, 1, 128),
 )
-STAGE2 = (dict(tile_subjects=32), dict(tile_subjects=128), dict(tile_subjects=512), dict(global_tables=True))
+STAGE2 = (dict(tile_subjects=32), dict(tile_subjects=128), dict(tile_subjects=512), dict(tile_bytes=4096),
+          dict(tile_bytes=16384), dict(tile_bytes=65536), dict(warps_per_subject=2), dict(warps_per_subject=4),
+          dict(warps_per_subject=8), dict(global_tables=True))
 
 
 @dataclass
@@ -54,7 +61,7 @@ class BucketResult:
 def time_choice(db: core.Database, pqs: Sequence[core.ProteinQuery], choice: Choice, db_residues: int,
                 reps: int = 2) -> float:
     batch = core.Batch.proteins(pqs, max_group_len=choice.max_group_len).set_mode(choice.mode)
-    batch.tune(choice.tile_subjects, choice.global_tables)
+    batch.tune(choice.tile_subjects, choice.global_tables).schedule(choice.warps_per_subject, choice.tile_bytes)
     s = core.Searcher(db, batch, core.default_options(num_threadsx=choice.threads))
     try:
         best = float("inf")
@@ -92,6 +99,8 @@ def tune(db: core.Database, queries: Sequence[core.ProteinQuery], db_residues: i
                 measure(c)
             first = br.best
             for kw in stage2:
+                if kw.get("warps_per_subject", 1) * 32 > first.threads:
+                    continue          # a pass shared by W groups needs W warps in the CTA
                 measure(replace(first, **kw))
         out.append(br)
     return out
@@ -128,7 +137,7 @@ def search_tuned(db: core.Database, queries: Sequence[core.ProteinQuery],
     wf = od = 0.0
     for c, idx in by_choice.items():
         batch = core.Batch.proteins([queries[i] for i in idx], max_group_len=c.max_group_len).set_mode(c.mode)
-        batch.tune(c.tile_subjects, c.global_tables)
+        batch.tune(c.tile_subjects, c.global_tables).schedule(c.warps_per_subject, c.tile_bytes)
         r = core.search(db, batch, core.default_options(num_threadsx=c.threads))
         h = r.hsps.copy()
         h["query"] = np.asarray(idx, dtype=np.int32)[h["query"]]

@@ -38,13 +38,19 @@ def test_blastp_and_blastx_files(built, tmp_path):
     nts = synth.blastx_queries(5, db, n_queries=3)
     fx = tmp_path / "x.fasta"
     fx.write_text("".join(f">x{i}\n" + "".join("ACGT"[c] for c in nt) + "\n" for i, nt in enumerate(nts)))
-    outx = tmp_path / "x.tsv"
-    assert hblastm.main(["-module", "blastx", "-query", str(fx), "-db", str(tmp_path / "db"), "-out", str(outx),
-                         "-screen_out", str(tmp_path / "x.log")]) == 0
-    want = []
     x6, c6 = np.full(6, 16, np.int32), np.full(6, 41, np.int32)
-    for i, nt in enumerate(nts):
-        prot, off, ln = oracle.translate6(nt)
-        pq = hblast.ProteinQuery(prot, off, ln, x6, c6)
-        want += lines_of(f"x{i}", hblast.search(gdb, hblast.Batch.proteins([pq])).hsps)
-    assert outx.read_text().splitlines() == want
+    # blastx masks its frames with SEG by default, as NCBI blastx does; -seg no searches them as they are
+    for seg in ("default", "no"):
+        outx = tmp_path / f"x_{seg}.tsv"
+        args = ["-module", "blastx", "-query", str(fx), "-db", str(tmp_path / "db"), "-out", str(outx),
+                "-screen_out", str(tmp_path / "x.log")] + ([] if seg == "default" else ["-seg", "no"])
+        assert hblastm.main(args) == 0
+        want = []
+        for i, nt in enumerate(nts):
+            prot, off, ln = oracle.translate6(nt)
+            if seg == "default":
+                for f in range(6):
+                    prot[off[f]:off[f] + ln[f]] = hblast.seg_mask(prot[off[f]:off[f] + ln[f]])
+            pq = hblast.ProteinQuery(prot, off, ln, x6, c6)
+            want += lines_of(f"x{i}", hblast.search(gdb, hblast.Batch.proteins([pq])).hsps)
+        assert len(want) > 0 and outx.read_text().splitlines() == want, seg
