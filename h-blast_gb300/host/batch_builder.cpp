@@ -152,7 +152,7 @@ std::string build_batch(const std::vector<QueryIn> &qs, int32_t threshold,
     if (qs.empty())
         return "empty batch";
     if (max_group_len <= 0)
-        max_group_len = std::max<int32_t>(1, kDefaultGroupTable - window);
+        max_group_len = kDefaultGroupLen;
     if (mode_hits < 0)
         mode_hits = kOffsetModeHits;
     HostBatch &b = *out;

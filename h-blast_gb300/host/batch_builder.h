@@ -20,11 +20,13 @@ namespace hbg {
 // warps to 8-20 per SM, and L2-resident global tables with 32 warps per SM
 // beat them by 13-23 % (4096 to 32768 entries, BLASTP and six-frame BLASTX).
 constexpr int32_t kSmemDiagMax = 2048;
-// Default group length: a full group's table is 4096 entries (global memory).
-// On the 64-query batched workload 4056-letter groups (16 scans of the
-// database) measured 4 % faster than 2008-letter groups in shared memory (37
-// scans), and 6000-letter groups 2 % slower.
-constexpr int32_t kDefaultGroupTable = 4096;
+// Default group length (letters, gaps included): a full group's table is 8192
+// entries of 16-bit cells in global memory.  On the 64-query batched workload
+// (GB300, word-finder ms for 2,000,000 subjects): groups of 6000 letters 906
+// (9 scans of the database), 7000 905, 8152 909, 4056 936 (16 scans), 10000
+// 942, 12000 975, 16344 1159 (the tables of all resident warps outgrow L2);
+// 2008-letter groups with shared tables are slower still (37 scans).
+constexpr int32_t kDefaultGroupLen = 6000;
 // Groups whose expected hits per subject offset reach this use offset mode
 // (off by default: chunk mode at high occupancy measured faster; the autotuner
 // and hbg_batch_set_mode choose offset mode explicitly).
