@@ -61,7 +61,7 @@ def test_schedule_knobs_keep_results(built):
     pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
     for glen in (0, 2008):
         ref = hblast.search(gdb, hblast.Batch.proteins(pqs, max_group_len=glen))
-        assert hblast.Batch.proteins(pqs, max_group_len=glen).info()["n_groups"] > 8
+        assert hblast.Batch.proteins(pqs, max_group_len=glen).info()["n_groups"] >= 5   # tiles of 3 groups leave a partial one
         for team, tb in ((2, 0), (3, 0), (8, 0), (1, 4096), (1, 65536), (8, 16384), (4, 1024)):
             r = hblast.search(gdb, hblast.Batch.proteins(pqs, max_group_len=glen).schedule(team, tb))
             assert np.array_equal(r.hsps, ref.hsps), (glen, team, tb)
