@@ -20,13 +20,17 @@ namespace hbg {
 // warps to 8-20 per SM, and L2-resident global tables with 32 warps per SM
 // beat them by 13-23 % (4096 to 32768 entries, BLASTP and six-frame BLASTX).
 constexpr int32_t kSmemDiagMax = 2048;
-// Default group length (letters, gaps included): a full group's table is 8192
-// entries of 16-bit cells in global memory.  On the 64-query batched workload
-// (GB300, word-finder ms for 2,000,000 subjects): groups of 6000 letters 906
-// (9 scans of the database), 7000 905, 8152 909, 4056 936 (16 scans), 10000
-// 942, 12000 975, 16344 1159 (the tables of all resident warps outgrow L2);
-// 2008-letter groups with shared tables are slower still (37 scans).
-constexpr int32_t kDefaultGroupLen = 6000;
+// Default group length (letters, gaps included): 4056, the longest whose
+// table is 4096 entries of 16-bit cells in global memory (8 KB a warp, 40 MB
+// for all resident warps, which stay in L2).  On the 64-query batched workload
+// (GB300, word-finder ms for 2,000,000 subjects): 4056 letters 936 (16 scans
+// of the database); 6000 906, 7000 905, 8152 909 (8192-entry tables: 80 MB,
+// which L2 no longer holds -- DRAM writes of evicted table lines rise from
+// 6.4 GB to 92 GB per 500,000 subjects, ~15x, for 3 % less time); 10000 942,
+// 12000 975, 16344 1159; 2008-letter groups with shared tables are slower
+// still (37 scans).  The autotuner picks longer groups per bucket when a
+// caller accepts the traffic.
+constexpr int32_t kDefaultGroupLen = 4056;
 // Groups whose expected hits per subject offset reach this use offset mode
 // (off by default: chunk mode at high occupancy measured faster; the autotuner
 // and hbg_batch_set_mode choose offset mode explicitly).
