@@ -531,9 +531,12 @@ __device__ __forceinline__ void scan_words(const Item<Cell> &it, Stage &stg, War
     }
 }
 
-// Chunk mode, for sparse groups: one (group, subject) item scanned 32
-// offsets at a time, the hits of the chunk compacted in CPU order and applied
-// 32 at a time.  Warp-collective.
+// Chunk mode: one (group, subject) item scanned 32 offsets at a time, the
+// hits of each chunk compacted in CPU order, and the subject's hit stream
+// applied 32 at a time across chunk boundaries: a chunk's last, partial batch
+// waits in lanes 0..carry-1 and is completed by the next chunk's first hits
+// (lane order stays CPU order), so only a subject's last batch runs partly
+// empty.  Warp-collective.
 template <typename Cell>
 __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs &a, Slot &sh,
                                            WarpQueue &wq, const uint32_t *cs, const uint16_t *ents,
@@ -544,6 +547,8 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
     unsigned long long item_hits = 0;
     Stage stg;
     stage_begin(stg, wq, it.s, it.S, lane);
+    uint32_t carry = 0;        // hits of earlier chunks not applied yet, in lanes 0..carry-1
+    int s_n = 0, q_n = 0;      // this lane's next hit: subject and group-local query offset
     // software pipeline: the next chunk's cell bounds are loaded while this
     // chunk's hits are applied, and each batch's query offsets while the
     // previous batch is applied
@@ -580,20 +585,31 @@ __device__ unsigned long long process_item(Item<Cell> &it, const WordFinderArgs 
             const uint32_t r = __shfl_sync(0xffffffffu, rel, lo);
             *q = h < T_ ? (int)__ldg(ents + (r + h)) : 0;
         };
-        int s_n = 0, q_n = 0;
-        if (T_ > 0)
-            locate((uint32_t)lane, &s_n, &q_n);
-        for (uint32_t hb = 0; hb < T_; hb += 32) {
-            const bool act = hb + lane < T_;
+        // the stream continues: position c = carry + h holds hit h of this chunk
+        const uint32_t total = carry + T_;
+        if (T_ > 0) {
+            int s_c, q_c;
+            locate((uint32_t)lane - carry, &s_c, &q_c);
+            if ((uint32_t)lane >= carry) {
+                s_n = s_c;
+                q_n = q_c;
+            }
+        }
+        uint32_t cb = 0;
+        for (; cb + 32 <= total; cb += 32) {       // full batches
             const int s_h = s_n, q = q_n;
-            if (hb + 32 < T_)
-                locate(hb + 32 + lane, &s_n, &q_n);
-            const int d = act ? ((q - s_h) & it.mask) : 0;
-            apply_hits(it, act, d, s_h, q, wq, n_tasks, n_blk, blk_cur);
+            if (cb + 32 < total)                   // positions >= 32 are hits of this chunk
+                locate(cb + 32 + lane - carry, &s_n, &q_n);
+            apply_hits(it, true, (q - s_h) & it.mask, s_h, q, wq, n_tasks, n_blk, blk_cur);
             // queues hold 64: keep room for one more batch of 32
             while (n_tasks >= 32 || n_blk >= 32)
                 flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, false);
         }
+        carry = total - cb;                        // these wait in (s_n, q_n) of lanes 0..carry-1
+    }
+    if (carry > 0) {                               // the subject's last batch
+        const bool act = (uint32_t)lane < carry;
+        apply_hits(it, act, act ? ((q_n - s_n) & it.mask) : 0, s_n, q_n, wq, n_tasks, n_blk, blk_cur);
     }
     flush(it, a, sh, wq, n_tasks, n_blk, blk_cur, true);
     stage_end();
