@@ -18,7 +18,10 @@
 //     least probable is kept: P0 = (N! / prod_k r_k!) (L! / prod_i n_i!) / N^L
 //     with N = 20, L its length, n_i its letter counts and r_k the number of
 //     letters that occur exactly k times.  Ties go to the leftmost, then the
-//     shortest subsequence.
+//     shortest subsequence.  The search trims at most kMaxTrim letters from
+//     each end of the raw segment (a bound of this implementation: the search
+//     is exhaustive for raw segments of up to 2 x kMaxTrim letters and linear
+//     in the length beyond, so a long low-complexity query stays cheap).
 //  4. The parts of the raw segment left and right of it are searched again
 //     with steps 1-3 as sequences of their own; then the scan resumes after
 //     the raw segment.
@@ -29,6 +32,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/hblast_gpu.h"
@@ -40,6 +44,7 @@ namespace {
 
 constexpr int kN = 20;
 constexpr uint8_t kMaskLetter = 21;   // X
+constexpr int32_t kMaxTrim = 100;     // letters the optimum may drop from each end of a raw segment
 
 // NCBIstdaa letter -> index among the 20 standard amino acids, -1 otherwise
 int std_index(uint8_t c) {
@@ -104,18 +109,21 @@ struct Seg {
         return v;
     }
 
-    // Least probable subsequence [*bi, *bj) of [a, b) (standard letters only).
+    // Least probable subsequence [*bi, *bj) of [a, b) (standard letters
+    // only) that starts within kMaxTrim letters of a and ends within kMaxTrim
+    // letters of b.
     void optimise(int32_t a, int32_t b, int32_t *bi, int32_t *bj) const {
         double best = INFINITY;
         *bi = a;
         *bj = b;
-        for (int32_t i = a; i < b; ++i) {
+        const int32_t i_end = std::min(b, a + kMaxTrim + 1);
+        for (int32_t i = a; i < i_end; ++i) {
+            const int32_t j_lo = std::max(i, b - kMaxTrim - 1);   // first end index j (inclusive) tried
             int cnt[kN] = {0};
-            for (int32_t j = i; j < b; ++j) {
-                const int x = std_index(s[j]);
-                if (x < 0)
-                    break;            // raw segments hold standard letters only
-                cnt[x]++;
+            for (int32_t j = i; j < j_lo; ++j)
+                cnt[std_index(s[j])]++;
+            for (int32_t j = j_lo; j < b; ++j) {
+                cnt[std_index(s[j])]++;
                 const double v = log_p0(cnt, j - i + 1);
                 if (v < best) {
                     best = v;

@@ -53,12 +53,17 @@ def log_p0(cnt, L: int) -> float:
     return v
 
 
+MAX_TRIM = 100    # the library's bound: at most 100 letters trimmed from each end of a raw segment
+
+
 def optimise(s, a: int, b: int):
     best, bi, bj = math.inf, a, b
-    for i in range(a, b):
+    for i in range(a, min(b, a + MAX_TRIM + 1)):
         cnt = [0] * N
         for j in range(i, b):
             cnt[IDX[int(s[j])]] += 1
+            if j < b - MAX_TRIM - 1:
+                continue
             v = log_p0(cnt, j - i + 1)
             if v < best:
                 best, bi, bj = v, i, j + 1

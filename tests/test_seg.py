@@ -48,6 +48,22 @@ def test_seg_matches_restatement(built, k):
     assert np.array_equal(hblast.seg_mask(s), seg_ref(s)), k
 
 
+def test_seg_long_raw_segments(built):
+    """Raw segments longer than the trimming bound (100 letters at each end):
+    the restatement agrees, and a 35,000-letter low-complexity query is masked
+    in well under a second."""
+    import time
+    rng = np.random.default_rng(8)
+    s = np.concatenate([synth.random_letters(rng, 50), rng.choice(enc("QQQQP"), size=260).astype(np.uint8),
+                        synth.random_letters(rng, 50)])
+    assert np.array_equal(hblast.seg_mask(s), seg_ref(s))
+    big = np.full(35000, enc("Q")[0], np.uint8)
+    t = time.perf_counter()
+    m = hblast.seg_mask(big)
+    assert time.perf_counter() - t < 1.0
+    assert (m == 21).all()
+
+
 def test_seg_parameters_matter(built):
     s = np.concatenate([synth.random_letters(np.random.default_rng(9), 60), enc("SGSGSGNSGSGSGGSNSG")])
     for w, lo, hi in ((12, 2.2, 2.5), (8, 1.5, 2.0), (20, 3.0, 3.3)):
