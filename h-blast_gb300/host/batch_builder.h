@@ -28,8 +28,9 @@ constexpr int32_t kSmemDiagMax = 2048;
 // which L2 no longer holds -- DRAM writes of evicted table lines rise from
 // 6.4 GB to 92 GB per 500,000 subjects, ~15x, for 3 % less time); 10000 942,
 // 12000 975, 16344 1159; 2008-letter groups with shared tables are slower
-// still (37 scans).  The autotuner picks longer groups per bucket when a
-// caller accepts the traffic.
+// still (37 scans).  Since each subject's hits are carried across chunks,
+// 6000-letter groups are within 0.4 % of 4056 (858 vs 862 ms), so the extra
+// traffic buys nothing.
 constexpr int32_t kDefaultGroupLen = 4056;
 // Groups whose expected hits per subject offset reach this use offset mode
 // (off by default: chunk mode at high occupancy measured faster; the autotuner
