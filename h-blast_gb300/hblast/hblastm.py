@@ -108,7 +108,7 @@ def main(argv=None) -> int:
     log = open(a.screen_out, "w") if a.screen_out else sys.stderr
     try:
         if a.gpu == "F":
-            print("hblastm: this build has no CPU path; -gpu F is not supported", file=log)
+            print("hblastm: this library has no CPU path; -gpu F is not supported", file=log)
             return 2
         ndev = core.device_count()
         if a.gpu_cards < 1 or a.method < 0 or a.method + a.gpu_cards > ndev:
