@@ -210,3 +210,25 @@ def test_blastx_seg_masked(built):
         pqs.append(hblast.ProteinQuery(prot, off, ln, xd[k], cu[k]))
     assert len(res.hsps) > 0
     check(res, pqs, db.residues, db.offsets)
+
+
+@pytest.mark.parametrize("threshold,window", [(12, 40), (13, 40), (11, 20), (11, 60)])
+def test_word_parameters(small_db, threshold, window):
+    """Other neighbourhood thresholds and two-hit windows (-threshold,
+    -window_size), against the oracle run with the same parameters."""
+    qs, db, gdb = small_db
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs, threshold=threshold, window=window))
+    h = res.hsps
+    assert len(h) > 0
+    for k, pq in enumerate(pqs):
+        ref, subj, cnt = oracle.search(oracle_query(pq), db.residues, db.offsets, threshold=threshold,
+                                       window=window, nthreads=4)
+        got = h[h["query"] == k]
+        assert len(got) == len(ref), (k, threshold, window)
+        assert np.array_equal(got["subject"], subj), k
+        for f, g in (("q_start", "q_start"), ("s_start", "s_start"), ("q_off", "q_off"), ("s_off", "s_off"),
+                     ("len", "len"), ("score", "score"), ("ctx", "context")):
+            assert np.array_equal(got[g], ref[f]), (k, f)
+        st = res.stats[k]
+        assert (st["lookup_hits"], st["init_extends"], st["good_init_extends"]) == tuple(int(c) for c in cnt), k
