@@ -880,8 +880,8 @@ cudaError_t wordfinder_configure() {
     // opt in to the largest shared-memory carve-out; launches size their own.
     // The global-table instantiations prefer a carve-out of ~40 % (four CTAs
     // need about 88 KB), leaving the rest of the SM's 256 KB to the L1 cache
-    // that holds their diagonal tables (measured 4 % faster than the driver's
-    // default choice); a hint the driver may round up.
+    // that holds their diagonal tables (measured 4 % faster than the CUDA
+    // driver's default choice); a hint the CUDA driver may round up.
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
