@@ -96,6 +96,38 @@ def test_both_hit_modes(small_db, mode):
     check(res, pqs, db.residues, db.offsets)
 
 
+def contexts_query(parts, x_dropoff, cutoff):
+    """Several sequences as the contexts of one query (one sentinel between
+    contexts), each with its own X-drop and cutoff."""
+    seq, off, ln, pos = [], [], [], 0
+    for k, p in enumerate(parts):
+        if k:
+            seq.append(np.zeros(1, np.uint8))
+            pos += 1
+        off.append(pos)
+        ln.append(len(p))
+        seq.append(p)
+        pos += len(p)
+    return hblast.ProteinQuery(np.concatenate(seq), off, ln, x_dropoff, cutoff)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_per_context_dropoff_and_cutoff(small_db, mode):
+    """X-drop and cutoff are per-context inputs (H-BLAST h_blast.cu:977-983):
+    contexts of one query with different values, in both hit modes."""
+    qs, db, gdb = small_db
+    pqs = [contexts_query([qs[0], qs[1], qs[3]], [7, 16, 30], [25, 41, 55]),
+           contexts_query([qs[2], qs[5]], [22, 10], [33, 60]),
+           contexts_query([qs[6], qs[7], qs[4]], [40, 12, 16], [41, 20, 41])]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs).set_mode(mode))
+    assert len(res.hsps) > 0
+    check(res, pqs, db.residues, db.offsets)
+    # the per-context values matter: the same contexts at 16 / 41 give other HSPs
+    flat = [contexts_query([qs[0], qs[1], qs[3]], [16] * 3, [41] * 3)]
+    ref = hblast.search(gdb, hblast.Batch.proteins(flat).set_mode(mode))
+    assert not np.array_equal(ref.hsps, res.hsps[res.hsps["query"] == 0])
+
+
 def test_blastx(built):
     rng = np.random.default_rng(13)
     prot_q = synth.random_letters(rng, 400)
