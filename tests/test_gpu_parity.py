@@ -163,6 +163,42 @@ def test_edge_subjects(built):
     check(res, pqs, residues, offsets)
 
 
+def test_full_alphabet(built):
+    """Queries and subjects drawn from all 27 NCBIstdaa letters (B, Z, X, U,
+    *, O and J included, about a quarter of the letters): words over the whole
+    28-letter index space and those letters' matrix rows and columns in the
+    walks.  A third of the subjects hold a mutated segment of a query, so
+    extensions pass the cutoff."""
+    rng = np.random.default_rng(15)
+    qs = [rng.integers(1, 28, size=n, dtype=np.uint8) for n in (200, 700, 31)]
+    subs = []
+    for i in range(1500):
+        s = rng.integers(1, 28, size=int(rng.integers(20, 400)), dtype=np.uint8)
+        if i % 3 == 0:
+            q = qs[i % 2]
+            a, n = int(rng.integers(0, len(q) - 60)), int(rng.integers(30, 60))
+            seg = q[a:a + n].copy()
+            mut = rng.random(n) < 0.2
+            seg[mut] = rng.integers(1, 28, size=int(mut.sum()), dtype=np.uint8)
+            p = int(rng.integers(0, len(s) + 1))
+            s = np.concatenate([s[:p], seg, s[p:]])
+        subs.append(s)
+    offsets = np.zeros(len(subs) + 1, np.int64)
+    offsets[1:] = np.cumsum([len(s) for s in subs])
+    residues = np.concatenate(subs)
+    gdb = hblast.Database(residues, offsets)
+    pqs = [hblast.ProteinQuery.blastp(q) for q in qs]
+    res = hblast.search(gdb, hblast.Batch.proteins(pqs))
+    h = res.hsps
+    assert len(h) > 100
+    check(res, pqs, residues, offsets)
+    # the HSPs run over the non-standard letters
+    nonstd = np.isin(residues, [2, 21, 23, 24, 25, 26, 27])
+    covered = sum(int(nonstd[offsets[r["subject"]] + r["s_start"]:offsets[r["subject"]] + r["s_start"] + r["len"]].sum())
+                  for r in h)
+    assert covered > 0
+
+
 def test_empty_database(built):
     gdb = hblast.Database(np.zeros(0, np.uint8), np.zeros(1, np.int64))
     res = hblast.search(gdb, hblast.Batch.proteins([hblast.ProteinQuery.blastp(np.ones(50, np.uint8))]))
