@@ -1,9 +1,9 @@
 """GPU word finder (through the C ABI) against the CPU oracle, bit-exact.
 
 Every HSP field and the per-query counters must be identical; tolerance 0
-(integer work).  Sizes are kept where the oracle finishes in seconds; the
-full-size configurations are covered by size-independent properties in
-test_gpu_fullsize.py.
+(integer work).  Sizes are kept where the oracle finishes in seconds (the
+plain configuration is whole); the full-size batched and BLASTX workloads are
+compared with the oracle in test_gpu_fullsize.py.
 """
 import numpy as np
 import pytest
