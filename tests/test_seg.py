@@ -70,6 +70,26 @@ def test_seg_parameters_matter(built):
         assert np.array_equal(hblast.seg_mask(s, w, lo, hi), seg_ref(s, w, lo, hi)), (w, lo, hi)
 
 
+def test_seg_idempotent(built):
+    """Masking a masked sequence again changes nothing: every window that
+    reaches into a masked stretch holds an X and cannot trigger, and the rest
+    is scanned as before.  Random proteins with planted stretches of one to
+    three letters."""
+    rng = np.random.default_rng(5)
+    masked = 0
+    for _ in range(200):
+        n = int(rng.integers(20, 600))
+        x = synth.random_letters(rng, n)
+        for _ in range(int(rng.integers(0, 4))):
+            a, ln = int(rng.integers(0, n)), int(rng.integers(5, 80))
+            alph = rng.integers(1, 21, size=int(rng.integers(1, 4)))
+            x[a:a + ln] = rng.choice(alph, size=len(x[a:a + ln]))
+        m = hblast.seg_mask(x)
+        masked += int((m != x).sum())
+        assert np.array_equal(hblast.seg_mask(m), m)
+    assert masked > 1000
+
+
 def test_seg_known_answers(built):
     rng = np.random.default_rng(4)
     q = synth.random_letters(rng, 300)
