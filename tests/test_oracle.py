@@ -108,6 +108,26 @@ def test_three_apart_extends_and_sets_flag(built):
     assert cnt == [8, 1, 1]
 
 
+@pytest.mark.parametrize("g", [7, 8])
+def test_xdrop_recovery_and_stop(built, g):
+    # Q = WWW G^g WWW, S = WWW P^g WWW, cell WWW = {0, g+3}: diagonal 0 has
+    # hits at s=0 and s=g+3.  Word W/W x 3 = 33, right_d 3, s_r = q_r = g+6.
+    # The left walk keeps 33 over the word, then loses 2 per G/P letter.
+    # g=7: the drop reaches 14 < 16, the walk goes on and recovers to
+    # 33 - 14 + 33 = 52 over all g+6 = 13 letters (it reaches the first hit,
+    # and the right walk has no letters left) -> HSP (0, 0, len 13, score 52).
+    # g=8: the eighth G/P letter makes the drop 16 (>= X-drop): the walk stops
+    # with 33 over 3 letters, short of the first hit, so no right walk; 33 < 41
+    # is not kept.
+    q = "WWW" + "G" * g + "WWW"
+    s = "WWW" + "P" * g + "WWW"
+    rows, cnt = run(q, s, {"WWW": [0, g + 3]}, cutoff=41)
+    if g == 7:
+        assert rows == [(0, 0, 10, 10, 13, 52, 0)] and cnt == [4, 1, 1]
+    else:
+        assert rows == [] and cnt == [4, 1, 0]
+
+
 def test_flag_suppresses_hits_inside_extension(built):
     # Same extension as above (every letter of S[6..15] scores -2 against G),
     # so the right walk ends at s_last_off = 13 and diagonal 0 is flagged with
