@@ -128,6 +128,24 @@ def test_xdrop_recovery_and_stop(built, g):
         assert rows == [] and cnt == [4, 1, 0]
 
 
+def test_right_walk_stops_at_zero(built):
+    # Q = GGG AAA G^10, S = PPP AAA PPPP KKK RRR; the hand table maps PPP->0,
+    # AAA->3, KKK->10, RRR->13 (whatever the query holds there).  Diagonal 0:
+    # hits at s=0 and s=3 (diff 3): word A/A x 3 = 12, s_r = 6; the left walk
+    # keeps those 3 letters (G/P = -2 before them) and reaches the first hit's
+    # end (3), so the right walk starts at 12 and loses 2 per letter (P/G, K/G):
+    # it stops at score 0 on its sixth letter (s_last_off 11; the X-drop of 16
+    # would only stop it two letters later), HSP (3, 3, len 3, score 12), and
+    # the diagonal is flagged up to 9.  So KKK at s=10 resets the diagonal and
+    # RRR at s=13 (diff 3) tries a second extension (R/G and K/G all -2:
+    # score 0, not kept).  With the walk stopped by the X-drop instead, the
+    # flag would reach 11, KKK would be skipped and RRR would only reset.
+    rows, cnt = run("GGGAAA" + "G" * 10, "PPPAAAPPPPKKKRRR",
+                    {"PPP": [0], "AAA": [3], "KKK": [10], "RRR": [13]}, cutoff=10)
+    assert rows == [(3, 3, 3, 3, 3, 12, 0)]
+    assert cnt == [6, 2, 1]
+
+
 def test_flag_suppresses_hits_inside_extension(built):
     # Same extension as above (every letter of S[6..15] scores -2 against G),
     # so the right walk ends at s_last_off = 13 and diagonal 0 is flagged with
