@@ -11,6 +11,7 @@ import pytest
 import hblast
 from hblast import synth
 from oracle import oracle
+from test_oracle import KNOWN_ANSWERS, enc, hand_lut
 
 pytestmark = pytest.mark.gpu
 
@@ -226,6 +227,28 @@ def test_smallbone_table(built):
     pq = hblast.ProteinQuery.blastp(q)
     res = hblast.search(gdb, hblast.Batch.from_smallbone(pq, cells, overflow))
     check(res, [pq], db.residues, db.offsets)
+
+
+@pytest.mark.parametrize("case", KNOWN_ANSWERS, ids=[c[0] for c in KNOWN_ANSWERS])
+def test_hand_derived_cases(built, case):
+    """The cases worked out by hand in test_oracle.py, on the GPU: the query's
+    lookup table is the hand-made one (passed as an NCBI smallbone table) and
+    the database is the case's one subject."""
+    from test_host import smallbone_from_csr
+    name, q, s, cells, xdrop, cutoff, rows, cnt = case
+    cells_bb, overflow = smallbone_from_csr(*hand_lut(cells))
+    sub = enc(s)
+    gdb = hblast.Database(sub, np.array([0, len(sub)], np.int64))
+    pq = hblast.ProteinQuery.blastp(enc(q), xdrop, cutoff)
+    res = hblast.search(gdb, hblast.Batch.from_smallbone(pq, cells_bb, overflow))
+    got = [tuple(int(h[f]) for f in ("q_start", "s_start", "q_off", "s_off", "len", "score", "context"))
+           for h in res.hsps]
+    st = res.stats[0]
+    if rows is not None:
+        assert got == rows, name
+    for g, w in zip((st["lookup_hits"], st["init_extends"], st["good_init_extends"]), cnt):
+        assert w is None or g == w, name
+    gdb.close()
 
 
 def test_launch_shapes_do_not_change_results(small_db):

@@ -47,6 +47,42 @@ def run(q: str, s: str, cells: dict, xdrop=16, cutoff=30):
     return rows, [int(c) for c in cnt]
 
 
+def window_case(D):
+    """Hits (0,0) and (D,D) on diagonal 0 of W-runs in G/P backgrounds."""
+    if D < 3:
+        return "W" * (D + 3) + "G" * 10, "W" * (D + 3) + "P" * 10
+    return "WWW" + "G" * (D - 3) + "WWW" + "G" * 10, "WWW" + "P" * (D - 3) + "WWW" + "P" * 10
+
+
+# The hand-derived cases of the tests below as one table, so that the GPU
+# tests can run the same cases with the same hand-made lookup tables:
+# (name, query, subject, cells, X-drop, cutoff, HSP rows, [lookup hits,
+# extensions, kept]); None where the answer is not worked out by hand.
+KNOWN_ANSWERS = [
+    ("runs", "A" * 10, "A" * 10, {"AAA": [0, 5]}, 16, 30,
+     [(0, 0, 5, 5, 10, 40, 0), (0, 1, 5, 6, 9, 36, 0), (0, 2, 5, 7, 8, 32, 0)], [16, 3, 3]),
+    ("three_apart", "W" * 6 + "G" * 10, "W" * 6 + "P" * 10, {"WWW": [0, 3]}, 16, 41,
+     [(0, 0, 3, 3, 6, 66, 0)], [8, 1, 1]),
+    ("flag", "W" * 6 + "G" * 10, "W" * 6 + "PPEHKPQRTP", {"WWW": [0, 3], "EHK": [8], "QRT": [12]}, 16, 41,
+     [(0, 0, 3, 3, 6, 66, 0)], [10, 1, 1]),
+    ("xdrop_recovers", "WWW" + "G" * 7 + "WWW", "WWW" + "P" * 7 + "WWW", {"WWW": [0, 10]}, 16, 41,
+     [(0, 0, 10, 10, 13, 52, 0)], [4, 1, 1]),
+    ("xdrop_stops", "WWW" + "G" * 8 + "WWW", "WWW" + "P" * 8 + "WWW", {"WWW": [0, 11]}, 16, 41, [], [4, 1, 0]),
+    ("right_walk_zero", "GGGAAA" + "G" * 10, "PPPAAAPPPPKKKRRR",
+     {"PPP": [0], "AAA": [3], "KKK": [10], "RRR": [13]}, 16, 10, [(3, 3, 3, 3, 3, 12, 0)], [6, 2, 1]),
+] + [("window_%d" % D, *window_case(D), {"WWW": [0, D]}, 16, 41, [] if D == 39 else None,
+      [None, int(3 <= D < 40), 0 if D == 39 else None]) for D in (2, 3, 39, 40, 41)]
+
+
+def test_known_answer_table(built):
+    for name, q, s, cells, xdrop, cutoff, rows, cnt in KNOWN_ANSWERS:
+        got_rows, got_cnt = run(q, s, cells, xdrop, cutoff)
+        if rows is not None:
+            assert got_rows == rows, name
+        for g, w in zip(got_cnt, cnt):
+            assert w is None or g == w, name
+
+
 def test_matrix_matches_reference(built):
     m = np.array(GOLD["blosum62_ncbistdaa_28x32"])
     for a in range(28):
@@ -83,12 +119,7 @@ def test_two_hits_on_runs(built):
 @pytest.mark.parametrize("D,extended", [(2, 0), (3, 1), (39, 1), (40, 0), (41, 0)])
 def test_window_boundaries(built, D, extended):
     # Hits (0,0) and (D,D) on diagonal 0: extend only when 3 <= D < 40.
-    if D < 3:
-        q = "W" * (D + 3) + "G" * 10
-        s = "W" * (D + 3) + "P" * 10
-    else:
-        q = "WWW" + "G" * (D - 3) + "WWW" + "G" * 10
-        s = "WWW" + "P" * (D - 3) + "WWW" + "P" * 10
+    q, s = window_case(D)
     rows, cnt = run(q, s, {"WWW": [0, D]}, cutoff=41)
     assert cnt[1] == extended
     if D == 39:
